@@ -1,0 +1,79 @@
+// Shared definitions of the GB300 execute path: element types, launch
+// bookkeeping and the CUDA error check used by every translation unit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <vector>
+
+#include "dtfft.h"
+
+namespace gb {
+
+typedef int64_t i64;
+
+// 16-byte element (complex<double>); the move kernels only copy it.
+struct __align__(16) e16 { uint64_t lo, hi; };
+
+// Number of this library's kernel launches since load (benchmark accounting).
+extern std::atomic<int64_t> g_launches;
+inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+#define GB_CUDA_TRY(expr)                                             \
+    do {                                                              \
+        cudaError_t e_ = (expr);                                      \
+        if (e_ != cudaSuccess) return DTFFT_ERROR_GPU_CALL_FAILED;    \
+    } while (0)
+
+#define GB_TRY(expr)                                                  \
+    do {                                                              \
+        dtfft_error_t r_ = (expr);                                    \
+        if (r_ != DTFFT_SUCCESS) return r_;                           \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Transposition boxes.
+//
+// A transpose of the virtual grid is a list of boxes, one per (source rank,
+// destination rank) pair whose global blocks intersect.  Inside a box, `a` is
+// the source's contiguous axis, `b` the destination's contiguous axis and `c`
+// the third axis:
+//     src[src_off + a + b*sb + c*sc]  ->  dst[dst_off + b + a*da + c*dc]
+// Boxes with a == b (plain copies) use the same struct with `copy` set:
+//     src[src_off + a + b*sb + c*sc]  ->  dst[dst_off + a + b*db + c*dc]
+// Offsets and strides are in elements, 64-bit: the whole grid lives in one
+// allocation that may exceed 2^31 elements.
+// ---------------------------------------------------------------------------
+struct Box {
+    i64 src_off, dst_off;
+    int32_t na, nb, nc;
+    int32_t tiles_a, tiles_b;   // tiles per c-plane (set by the launcher)
+    i64 sb, sc;                 // source strides of b and c
+    i64 da_or_db, dc;           // destination stride of a (transpose) or b (copy), and of c
+    i64 tile_begin;             // first global tile index of this box
+};
+
+// Kernel launch choice for a box list (autotuned or default).
+struct TransposeConfig {
+    int tile_a = 32;   // tile extent along the source-contiguous axis
+    int tile_b = 32;   // tile extent along the destination-contiguous axis
+    int rows = 8;      // thread rows per CTA (blockDim.y)
+};
+
+// Device-resident box list of one data movement.
+struct BoxList {
+    std::vector<Box> host;
+    Box* dev = nullptr;
+    i64 total_tiles = 0;
+    bool copy = false;        // all boxes are copies (a == b)
+    int elem = 8;             // element size in bytes
+    TransposeConfig cfg;
+};
+
+dtfft_error_t boxes_upload(BoxList& bl);
+void boxes_free(BoxList& bl);
+dtfft_error_t boxes_launch(const BoxList& bl, const void* in, void* out, cudaStream_t stream);
+
+}  // namespace gb

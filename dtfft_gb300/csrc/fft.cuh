@@ -1,0 +1,62 @@
+// Batched FFT executor of the GB300 execute path (replaces the cuFFT / VkFFT
+// executors of src/interfaces/fft/ behind src/dtfft_abstract_executor.F90).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace gb {
+
+enum FftType { FFT_C2C = 0, FFT_R2C = 1, FFT_R2R = 2 };
+enum { FFT_FWD = -1, FFT_BWD = 1 };  // src/include/_dtfft_private.h:27-28
+
+// One batched transform of rank 1 or 2 over contiguous rows.
+//  rank 1: `batch` signals of n_fast points, consecutive signals idist/odist
+//          elements apart (elements of the input / output type).
+//  rank 2: `batch` planes of n_slow x n_fast points (n_fast contiguous).
+//  R2C: input real rows of n_fast, output complex rows of n_fast/2+1; the
+//       backward direction is C2R.
+struct FftDesc {
+    int type = FFT_C2C;
+    int dbl = 0;
+    int rank = 1;
+    int n_fast = 1, n_slow = 1;
+    i64 batch = 0;
+    i64 idist = 0, odist = 0;
+    int kind_fast = 0, kind_slow = 0;  // dtfft_r2r_kind_t for FFT_R2R
+};
+
+// Radix schedule of one complex transform of length m (Stockham stages).
+struct Schedule {
+    int m = 1;
+    std::vector<int> radix;
+    std::string str() const;
+};
+bool make_schedule(int m, Schedule& s);
+
+struct FftStep;  // one kernel launch of a plan
+
+class FftPlan {
+public:
+    static dtfft_error_t create(const FftDesc& d, FftPlan** out);
+    ~FftPlan();
+    // in -> out; in == out allowed except for R2C / C2R.
+    dtfft_error_t execute(const void* in, void* out, int sign, cudaStream_t s);
+    const FftDesc& desc() const { return d_; }
+    int launches_per_execute() const { return launches_; }
+
+private:
+    FftDesc d_;
+    std::vector<FftStep*> fwd_, bwd_;
+    std::vector<void*> tables_;
+    int launches_ = 0;
+    dtfft_error_t build(int sign, std::vector<FftStep*>& steps);
+    dtfft_error_t twiddles(int m, const void** table);
+};
+
+}  // namespace gb

@@ -1,0 +1,140 @@
+/*
+ * dtfft_gb300.h -- entry points of libdtfft_gb300.so beyond the public
+ * dtfft.h ABI.
+ *
+ * 1. Kernel and executor plug-ins.  These are the two seams inside the
+ *    reference where its Fortran plan code calls into device code; a
+ *    Fortran build of dtFFT binds them with iso_c_binding (INTEGRATION.md
+ *    shows the interface blocks) in place of its NVRTC kernels and its cuFFT /
+ *    VkFFT executors.
+ *
+ * 2. Virtual-rank queries for plans whose communicator is a grid made by
+ *    dtfft_vgrid_cart_create: where each rank's block sits in the one device
+ *    buffer that holds all ranks.
+ *
+ * All functions return dtfft_error_t codes (dtfft.h).
+ */
+#ifndef DTFFT_GB300_H
+#define DTFFT_GB300_H
+
+#include "dtfft.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Kernel plug-in                                                            */
+/* Replaces kernel_device (src/dtfft_kernel_device.F90:61-178) behind        */
+/* abstract_kernel%create/execute/destroy (src/dtfft_abstract_kernel.F90).   */
+/* ------------------------------------------------------------------------ */
+
+/** Kernel types, numbered as the reference's kernel_type_t
+ * (src/dtfft_abstract_kernel.F90:61-97). */
+typedef enum {
+    GB_KERNEL_DUMMY = -1,
+    GB_KERNEL_PACK = 1,
+    GB_KERNEL_COPY_PIPELINED = 2,
+    GB_KERNEL_UNPACK = 3,
+    GB_KERNEL_COPY = 4,
+    GB_KERNEL_UNPACK_PIPELINED = 5,
+    GB_KERNEL_PACK_PIPELINED = 6,
+    GB_KERNEL_PERMUTE_FORWARD = 7,
+    GB_KERNEL_PERMUTE_BACKWARD = 8,
+    GB_KERNEL_PERMUTE_BACKWARD_START = 9,
+    GB_KERNEL_PERMUTE_BACKWARD_END = 10,
+    GB_KERNEL_PERMUTE_BACKWARD_END_PIPELINED = 11
+} gb_kernel_type_t;
+
+typedef struct gb_kernel_s* gb_kernel_t;
+
+/**
+ * Creates a local data-movement kernel.
+ * Reference: abstract_kernel%create(dims, effort, base_storage, kernel_type,
+ * neighbor_data, force_effort), src/dtfft_abstract_kernel.F90:220-285.
+ *
+ * @param ndims          2 or 3
+ * @param dims           local dims, fastest first
+ * @param base_storage   element size in bytes: 4, 8 or 16
+ * @param kernel_type    gb_kernel_type_t
+ * @param neighbor_data  5 x n_neighbors ints {n1, n2, n3, in_displ, out_displ}
+ *                       per neighbour (src/dtfft_reshape_handle_generic.F90:401-410),
+ *                       NULL for the permute kernels
+ * @param n_neighbors    number of neighbour columns
+ * @param effort         dtfft_effort_t; DTFFT_EXHAUSTIVE times the tile candidates
+ */
+dtfft_error_t gb_kernel_create(int32_t ndims, const int32_t* dims, int32_t base_storage,
+                               int32_t kernel_type, const int32_t* neighbor_data,
+                               int32_t n_neighbors, int32_t effort, gb_kernel_t* kernel);
+
+/**
+ * Enqueues the kernel on `stream` (a cudaStream_t, NULL = legacy default).
+ * Reference: abstract_kernel%execute(in, out, stream, neighbor),
+ * src/dtfft_abstract_kernel.F90:287-330.  `neighbor` is 1-based for the
+ * *_PIPELINED kernels and ignored otherwise.
+ */
+dtfft_error_t gb_kernel_execute(gb_kernel_t kernel, const void* in, void* out, void* stream, int32_t neighbor);
+
+dtfft_error_t gb_kernel_destroy(gb_kernel_t* kernel);
+
+/* ------------------------------------------------------------------------ */
+/* FFT executor plug-in                                                      */
+/* Replaces cufft_executor / vkfft_executor behind abstract_executor         */
+/* (src/dtfft_abstract_executor.F90:47-112, create_private/execute_private). */
+/* ------------------------------------------------------------------------ */
+
+typedef enum { GB_FFT_C2C = 0, GB_FFT_R2C = 1, GB_FFT_R2R = 2 } gb_fft_type_t;
+typedef enum { GB_FFT_FORWARD = -1, GB_FFT_BACKWARD = 1 } gb_fft_sign_t;
+
+typedef struct gb_fft_s* gb_fft_t;
+
+/**
+ * Creates a batched FFT along contiguous data, with the arguments the
+ * reference hands to its executors (src/dtfft_abstract_executor.F90:115-216):
+ * fft_sizes/inembed/onembed in FFTW's slowest-first order, unit stride,
+ * `idist`/`odist` between consecutive transforms.
+ *
+ * @param fft_rank    1 or 2
+ * @param fft_type    gb_fft_type_t
+ * @param precision   dtfft_precision_t
+ * @param r2r_kinds   fft_rank kinds for GB_FFT_R2R (slowest first), else NULL
+ * @param stream      cudaStream_t the transforms are enqueued on
+ */
+dtfft_error_t gb_fft_create(int32_t fft_rank, int32_t fft_type, int32_t precision, int32_t idist,
+                            int32_t odist, int32_t how_many, const int32_t* fft_sizes,
+                            const int32_t* inembed, const int32_t* onembed,
+                            const int32_t* r2r_kinds, void* stream, gb_fft_t* fft);
+
+/**
+ * Runs the transform a -> b (a == b allowed except for R2C/C2R).
+ * sign = GB_FFT_FORWARD: C2C forward, R2C, or R2R with the plan's kinds;
+ * sign = GB_FFT_BACKWARD: C2C backward, C2R, or R2R with the inverse kinds.
+ * Unnormalised, like FFTW.
+ */
+dtfft_error_t gb_fft_execute(gb_fft_t fft, void* a, void* b, int32_t sign);
+
+dtfft_error_t gb_fft_destroy(gb_fft_t* fft);
+
+/* ------------------------------------------------------------------------ */
+/* Virtual ranks                                                             */
+/* ------------------------------------------------------------------------ */
+
+/** Number of virtual ranks of the plan's grid (1 for MPI_COMM_WORLD plans). */
+dtfft_error_t dtfft_vgrid_get_nranks(dtfft_plan_t plan, int32_t* nranks);
+
+/**
+ * Pencil of virtual rank `vrank` in `layout` (what dtfft_get_pencil returns on
+ * that rank of an MPI run) and the element offset of that rank's block in a
+ * buffer holding `layout` for all ranks.  For R2C plans the X_PENCILS offset
+ * counts real elements and the others complex elements.
+ */
+dtfft_error_t dtfft_vgrid_get_pencil(dtfft_plan_t plan, dtfft_layout_t layout, int32_t vrank,
+                                     dtfft_pencil_t* pencil, size_t* offset);
+
+/** Number of launches of this library's kernels since load (for benchmarks). */
+int64_t dtfft_gb_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DTFFT_GB300_H */

@@ -1,0 +1,67 @@
+/*
+ * dtfft_mpi_shim.h -- the MPI names dtfft.h needs, for a library that runs
+ * every rank of a decomposition on one GPU.
+ *
+ * dtFFT's C ABI takes an `MPI_Comm` (include/dtfft.h:397-515 of the
+ * reference).  This library is a single process: it never calls MPI, so a
+ * communicator is only a handle that names a decomposition grid.
+ *
+ *   MPI_COMM_WORLD            one process, the grid is chosen by the planner
+ *   dtfft_vgrid_cart_create   a cartesian grid of virtual ranks, the way
+ *                             MPI_Cart_create(MPI_COMM_WORLD, ndims, dims, ...)
+ *                             would build it for prod(dims) processes
+ *
+ * Handles follow the MPICH ABI (MPI_Comm is a 32-bit int), which is also what
+ * the reference's Fortran layer receives (MPI_Comm_c2f, dtfft_api_c.c:42).
+ * Define DTFFT_HAVE_REAL_MPI and include <mpi.h> first to use a real MPI's
+ * MPI_Comm type instead; handles are then compared by value only.
+ */
+#ifndef DTFFT_MPI_SHIM_H
+#define DTFFT_MPI_SHIM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef DTFFT_HAVE_REAL_MPI
+typedef int MPI_Comm;
+#ifndef MPI_COMM_WORLD
+#define MPI_COMM_WORLD ((MPI_Comm)0x44000000)
+#endif
+#ifndef MPI_COMM_SELF
+#define MPI_COMM_SELF ((MPI_Comm)0x44000001)
+#endif
+#endif
+
+/**
+ * Creates a handle for a cartesian grid of virtual ranks.
+ *
+ * @param[in]  ndims  number of grid dimensions (1, 2 or 3)
+ * @param[in]  dims   grid sizes in the order MPI_Cart_create takes them;
+ *                    when ndims equals the plan's rank, dims[0] describes the
+ *                    fastest (X) axis and must be 1 for a plan (dtFFT's rule)
+ * @param[out] comm   handle to pass to dtfft_create_plan_*
+ * @return 0 on success, DTFFT_ERROR_INVALID_COMM_DIMS-like code otherwise
+ *
+ * Virtual rank r has cartesian coordinates in row-major order, exactly as
+ * MPI numbers the ranks of a cartesian communicator.
+ */
+int32_t dtfft_vgrid_cart_create(int32_t ndims, const int32_t* dims, MPI_Comm* comm);
+
+/**
+ * Creates a handle for `nprocs` virtual ranks without a topology, the way
+ * MPI_COMM_WORLD of an `nprocs`-process run looks to the planner: the plan
+ * then chooses the grid itself (Z-slab, Y-slab or a balanced P1 x P2 grid)
+ * by the reference's rules.
+ */
+int32_t dtfft_vgrid_world_create(int32_t nprocs, MPI_Comm* comm);
+
+/** Releases a handle made by dtfft_vgrid_cart_create or dtfft_vgrid_world_create. */
+int32_t dtfft_vgrid_free(MPI_Comm* comm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DTFFT_MPI_SHIM_H */

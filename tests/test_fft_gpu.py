@@ -1,0 +1,225 @@
+"""GPU parity of the FFT path: dtfft_execute through the C ABI against the
+FP64 oracle (FFTW conventions).
+
+Tolerances (relative L2 against the FP64 oracle): 1e-5 for single precision,
+1e-12 for double precision.  Round trips (forward, scale by 1/N, backward) are
+also held to the reference's max-abs threshold 5*log2(N)*eps
+(tests/test_utils.F90:89-109), with the scale conventions of
+tests/python/test_r2r_kinds_py.py for R2R kinds."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from gpu_util import comm_for, empty, from_dev, random_global, to_dev
+
+pytestmark = pytest.mark.gpu
+
+TOL = {np.complex64: 1e-5, np.complex128: 1e-12, np.float32: 1e-5, np.float64: 1e-12}
+
+
+def _prec(dt, np_dtype):
+    return dt.Precision.SINGLE if np_dtype in (np.complex64, np.float32) else dt.Precision.DOUBLE
+
+
+def _final_layout(plan, nd):
+    return 2 if (nd == 2 or plan.y_slab_enabled) else 3
+
+
+C2C_CASES = [
+    ([256, 256], [1, 1], np.complex128),            # 2D C2C c128 256x256, one process
+    ([64, 48, 40], [1, 2, 4], np.complex64),         # 2x4 grid, generic schedule
+    ([60, 45, 42], [1, 1, 1], np.complex64),         # Z-slab, radices 3/5/7
+    ([17, 23, 11], [1, 1, 1], np.complex64),         # odd primes (generic schedule, nz < 32)
+    ([48, 36, 40], [1, 3, 2], np.complex128),
+    ([96, 80, 64], [1, 1, 4], np.complex64),         # Z-slab on 4 ranks
+    ([31, 44], [1, 3], np.complex64),
+    ([512, 24], [1, 1], np.complex64),
+]
+
+
+@pytest.mark.parametrize("dims,grid,np_dtype", C2C_CASES)
+def test_c2c_forward_backward(dt, orc, cuda, dims, grid, np_dtype):
+    nd = len(dims)
+    plan = dt.PlanC2C(dims, comm=comm_for(dt, grid), precision=_prec(dt, np_dtype), executor=dt.Executor.CUFFT)
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=sum(dims))
+    x = orc.global_to_packed(g, nd, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    lay = _final_layout(plan, nd)
+    expect = orc.global_to_packed(orc.forward_values(g, "c2c"), nd, grid, lay)
+    out = from_dev(b, expect.size, np_dtype)
+    assert orc.rel_l2(out, expect) <= TOL[np_dtype]
+    c = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    back = from_dev(c, x.size, np_dtype).astype(np.complex128) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= TOL[np_dtype]
+    thr = orc.roundtrip_threshold(int(np.prod(dims)), np_dtype == np.complex64)
+    assert np.max(np.abs(back - x)) <= thr
+    plan.destroy()
+
+
+def test_c2c_schedules_agree(dt, orc, cuda):
+    """Z-slab, Y-slab and the generic 3-pencil schedule give the same spectrum."""
+    dims = [64, 64, 64]
+    g = random_global(tuple(dims[::-1]), np.complex64, seed=3)
+    expect = orc.forward_values(g, "c2c")
+    for zs, ys in ((True, False), (False, True), (False, False)):
+        cfg = dt.Config(enable_z_slab=zs, enable_y_slab=ys)
+        plan = dt.PlanC2C(dims, precision=dt.Precision.SINGLE, executor=dt.Executor.VKFFT, config=cfg)
+        assert plan.z_slab_enabled == zs and plan.y_slab_enabled == (ys and not zs)
+        x = orc.global_to_packed(g, 3, [1, 1, 1], 1)
+        a = to_dev(x, plan.alloc_size, cuda)
+        b = empty(plan.alloc_size, np.complex64, cuda)
+        plan.execute(a, b, dt.Execute.FORWARD)
+        lay = _final_layout(plan, 3)
+        out = from_dev(b, x.size, np.complex64)
+        assert orc.rel_l2(out, orc.global_to_packed(expect, 3, [1, 1, 1], lay)) <= 1e-5
+        plan.destroy()
+    dt.set_config(dt.Config())
+
+
+R2C_CASES = [
+    ([32, 24, 40], [1, 1, 1], np.float32),
+    ([16, 32, 70], [1, 1, 1], np.float64),           # tests/c/test_r2c_3d_c.c sizes
+    ([33, 20, 12], [1, 2, 2], np.float32),           # odd nx
+    ([64, 32, 36], [1, 4, 4], np.float64),           # 4x4 grid, 33 complex split unevenly
+    ([30, 26], [1, 1], np.float32),
+    ([21, 16], [1, 2], np.float64),
+]
+
+
+@pytest.mark.parametrize("dims,grid,np_dtype", R2C_CASES)
+def test_r2c_forward_backward(dt, orc, cuda, dims, grid, np_dtype):
+    nd = len(dims)
+    cdt = np.complex64 if np_dtype == np.float32 else np.complex128
+    plan = dt.PlanR2C(dims, comm=comm_for(dt, grid), precision=_prec(dt, np_dtype), executor=dt.Executor.CUFFT)
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=sum(dims), dist="normal")
+    x = orc.global_to_packed(g, nd, grid, 1)
+    n_real = plan.alloc_size
+    a = to_dev(x, n_real, cuda)
+    b = empty(n_real // 2 + 1, cdt, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    lay = _final_layout(plan, nd)
+    G = orc.forward_values(g, "r2c")
+    expect = orc.global_to_packed(G, nd, grid, lay)
+    out = from_dev(b, expect.size, cdt)
+    assert orc.rel_l2(out, expect) <= TOL[np_dtype]
+    c = empty(n_real, np_dtype, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    back = from_dev(c, x.size, np_dtype).astype(np.float64) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= TOL[np_dtype]
+    plan.destroy()
+
+
+KINDS = [(5, 5), (4, 4), (3, 3), (6, 6), (7, 7), (9, 9), (8, 8), (10, 10)]
+
+
+@pytest.mark.parametrize("kinds", KINDS)
+@pytest.mark.parametrize("np_dtype", [np.float64, np.float32])
+def test_r2r_kinds_roundtrip_17x23(dt, orc, cuda, kinds, np_dtype):
+    """tests/python/test_r2r_kinds_py.py: 17 x 23, every kind, FFTW scale conventions."""
+    nx, ny = 17, 23
+    plan = dt.PlanR2R([nx, ny], kinds=list(kinds), precision=_prec(dt, np_dtype), executor=dt.Executor.VKFFT)
+    g = random_global((ny, nx), np_dtype, seed=kinds[0])
+    x = orc.global_to_packed(g, 2, [1, 1], 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    expect = orc.global_to_packed(orc.forward_values(g, "r2r", kinds=list(kinds)), 2, [1, 1], 2)
+    out = from_dev(b, expect.size, np_dtype)
+    assert orc.rel_l2(out, expect) <= TOL[np_dtype]
+    plan.execute(b, a, dt.Execute.BACKWARD)
+    back = from_dev(a, x.size, np_dtype).astype(np.float64) / orc.r2r_roundtrip_scale([nx, ny], kinds)
+    atol = 1e-10 if np_dtype == np.float64 else 2e-5
+    assert np.max(np.abs(back - x)) <= atol
+    plan.destroy()
+
+
+@pytest.mark.parametrize("dims,grid,kinds", [
+    ([16, 24, 32], [1, 1, 1], (5, 5, 5)),           # Z-slab: 2D kinds (X, Y) then Z
+    ([16, 12, 20], [1, 2, 2], (5, 4, 6)),
+    ([9, 10, 12], [1, 1, 1], (3, 7, 9)),
+    ([64, 32, 40], [1, 4, 4], (10, 8, 5)),
+])
+def test_r2r_3d(dt, orc, cuda, dims, grid, kinds):
+    plan = dt.PlanR2R(dims, kinds=list(kinds), comm=comm_for(dt, grid), precision=dt.Precision.DOUBLE,
+                      executor=dt.Executor.VKFFT)
+    g = random_global(tuple(dims[::-1]), np.float64, seed=9, dist="normal")
+    x = orc.global_to_packed(g, 3, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, np.float64, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    lay = _final_layout(plan, 3)
+    expect = orc.global_to_packed(orc.forward_values(g, "r2r", kinds=list(kinds)), 3, grid, lay)
+    assert orc.rel_l2(from_dev(b, expect.size, np.float64), expect) <= 1e-12
+    plan.execute(b, a, dt.Execute.BACKWARD)
+    back = from_dev(a, x.size, np.float64) / orc.r2r_roundtrip_scale(dims, kinds)
+    assert np.max(np.abs(back - x)) <= 1e-10
+    plan.destroy()
+
+
+def test_r2r_with_cufft_executor_is_refused(dt):
+    with pytest.raises(dt.DtfftError) as e:
+        dt.PlanR2R([16, 16], kinds=[5, 5], executor=dt.Executor.CUFFT)
+    assert e.value.code == 101
+
+
+def test_r2c_transpose_only_execute_refused(dt, cuda):
+    import torch
+    plan = dt.PlanR2C([16, 16, 16], precision=dt.Precision.SINGLE)
+    a = torch.zeros(plan.alloc_size, dtype=torch.float32, device=cuda)
+    b = torch.zeros_like(a)
+    with pytest.raises(dt.DtfftError) as e:
+        plan.execute(a, b, dt.Execute.FORWARD)
+    assert e.value.code == 45
+    plan.destroy()
+
+
+# ---- FFT plug-in (gb_fft_*), the executor seam ------------------------------
+
+@pytest.mark.parametrize("n,howmany", [(256, 64), (768, 9), (17, 5), (1000, 3), (2048, 4)])
+def test_fft_plugin_c2c(dt, cuda, n, howmany):
+    import torch
+    L = dt.lib()
+    h = ctypes.c_void_p()
+    sizes = (ctypes.c_int32 * 1)(n)
+    assert L.gb_fft_create(1, 0, 0, n, n, howmany, sizes, sizes, sizes, None, None, ctypes.byref(h)) == 0
+    rng = np.random.default_rng(n)
+    x = (rng.uniform(-1, 1, (howmany, n)) + 1j * rng.uniform(-1, 1, (howmany, n))).astype(np.complex64)
+    a = torch.from_numpy(x).to(cuda)
+    b = torch.empty_like(a)
+    assert L.gb_fft_execute(h, a.data_ptr(), b.data_ptr(), -1) == 0
+    torch.cuda.synchronize()
+    ref = np.fft.fft(x.astype(np.complex128), axis=1)
+    err = np.linalg.norm(b.cpu().numpy() - ref) / np.linalg.norm(ref)
+    assert err <= 1e-5
+    assert L.gb_fft_execute(h, b.data_ptr(), b.data_ptr(), 1) == 0   # in place, backward
+    torch.cuda.synchronize()
+    back = b.cpu().numpy() / n
+    assert np.linalg.norm(back - x) / np.linalg.norm(x) <= 1e-5
+    assert L.gb_fft_destroy(ctypes.byref(h)) == 0
+
+
+@pytest.mark.parametrize("n", [64, 30, 31])
+def test_fft_plugin_r2c(dt, cuda, n):
+    import torch
+    L = dt.lib()
+    h = ctypes.c_void_p()
+    sizes = (ctypes.c_int32 * 1)(n)
+    onembed = (ctypes.c_int32 * 1)(n // 2 + 1)
+    howmany = 7
+    assert L.gb_fft_create(1, 1, 1, n, n // 2 + 1, howmany, sizes, sizes, onembed, None, None, ctypes.byref(h)) == 0
+    x = np.random.default_rng(n).standard_normal((howmany, n))
+    a = torch.from_numpy(x).to(cuda)
+    b = torch.empty((howmany, n // 2 + 1), dtype=torch.complex128, device=cuda)
+    assert L.gb_fft_execute(h, a.data_ptr(), b.data_ptr(), -1) == 0
+    torch.cuda.synchronize()
+    ref = np.fft.rfft(x, axis=1)
+    assert np.linalg.norm(b.cpu().numpy() - ref) / np.linalg.norm(ref) <= 1e-12
+    c = torch.empty_like(a)
+    assert L.gb_fft_execute(h, b.data_ptr(), c.data_ptr(), 1) == 0
+    torch.cuda.synchronize()
+    assert np.linalg.norm(c.cpu().numpy() / n - x) / np.linalg.norm(x) <= 1e-12
+    L.gb_fft_destroy(ctypes.byref(h))
