@@ -1,0 +1,331 @@
+"""Benchmark of dtFFT's execute path on GB300.
+
+Workload (headline): 3D C2C complex64 512 x 512 x 512 on a 2 x 4 virtual rank
+grid (8 pencil ranks held in one HBM allocation, 1 GiB per buffer), inputs
+uniform[-1,1) re/im.  One step = one forward + one backward dtfft_execute
+(X -> Y -> Z and back: 3 FFT passes + 2 transposes each way).
+
+JSON line (rank 0): metric / value (fwd+bwd cycles per second, whole job),
+roofline of the dominant kernel (live CUDA-event timing inside the timed
+region), e2e (same metric through the C ABI with host buffers and the
+host<->device copies inside the timed region), cpu_baseline (the CPU port of
+the reference path on the host cores), clocks sampled during the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs N independent replicas of the workload (one per GPU); the path is
+a single-GPU path with no inter-GPU exchange, so scaling is weak.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "3D fwd+bwd cycles/s & HBM TB/s; batched/TC vs plain on 1 GB300 at stated rel err"
+DIMS = [512, 512, 512]
+GRID = [1, 2, 4]
+WORKLOAD = "c2c_c64_512x512x512_grid2x4_fwd+bwd"
+FALLBACK_HBM = 6800.0
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def _profile_results(L):
+    out = []
+    n = L.dtfft_gb_profile_count()
+    for i in range(n):
+        name = ctypes.create_string_buffer(128)
+        launches = ctypes.c_int64()
+        ms = ctypes.c_double()
+        L.dtfft_gb_profile_get(i, name, 128, ctypes.byref(launches), ctypes.byref(ms))
+        out.append((name.value.decode(), int(launches.value), float(ms.value)))
+    return out
+
+
+def _traffic_for(kernel: str):
+    """dram read+write bytes per launch of `kernel` from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            t = json.load(f)
+        return t.get(WORKLOAD, {}).get(kernel)
+    except Exception:
+        return None
+
+
+def cpu_baseline(sample_seconds=12.0):
+    """The CPU port of the reference path, timed on this host (rank 0, N=1 only)."""
+    from oracle import cpu_execute
+    spc, cycles, threads = cpu_execute.time_cycles(DIMS, GRID, min_seconds=sample_seconds, max_cycles=2)
+    return {"value": 1.0 / spc, "unit": "cycles/s", "cores": threads, "kind": "port",
+            "sample": f"{cycles} full fwd+bwd cycle(s) of the {WORKLOAD} workload; C restatement of the "
+                      f"reference host kernels (OpenMP) + scipy.fft (pocketfft) for the FFTW executor"}
+
+
+def run_reference(args):
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return 0
+    from oracle import cpu_execute
+    steps = max(1, min(args.steps, 3))
+    warm = min(args.warmup, 1)
+    if warm:
+        cpu_execute.time_cycles(DIMS, GRID, min_seconds=1e9, max_cycles=warm)
+    spc, cycles, threads = cpu_execute.time_cycles(DIMS, GRID, min_seconds=1e9, max_cycles=steps)
+    v = 1.0 / spc
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cycles/s", "n_gpus": args.gpus,
+            "steps": cycles, "warmup": warm, "ms_per_step": spc * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "dims": DIMS, "grid": "1x2x4", "precision": "single",
+                       "executor": "CPU port (oracle/_build C kernels + scipy.fft)"},
+            "cpu_baseline": {"value": v, "unit": "cycles/s", "cores": threads, "kind": "port",
+                             "sample": f"{cycles} full fwd+bwd cycle(s) per timed run, {threads} host threads"},
+            "e2e": {"value": v, "unit": "cycles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import dtfft_gb300 as dt
+
+    rank, world, local = _env_rank()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = dt.lib()
+
+    global DIMS, GRID, WORKLOAD
+    if args.dims:
+        DIMS = list(args.dims)
+        GRID = [1] + list(args.grid)
+        WORKLOAD = f"c2c_c64_{'x'.join(map(str, DIMS))}_grid{'x'.join(map(str, GRID[1:]))}_fwd+bwd"
+    comm = dt.cart_comm(GRID)
+    # one stream for torch's copies and the plan's kernels
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    cfg = dt.Config(stream=stream.cuda_stream)
+    plan = dt.PlanC2C(DIMS, comm=comm, precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT,
+                      effort=dt.Effort(args.effort), config=cfg)
+    dt.set_config(dt.Config())
+    n = plan.alloc_size
+    nbytes = n * 8
+    g = torch.Generator(device=dev)
+    g.manual_seed(2)
+    x0 = torch.complex(torch.rand(n, device=dev, generator=g) * 2 - 1,
+                       torch.rand(n, device=dev, generator=g) * 2 - 1).to(torch.complex64)
+    a = x0.clone()
+    b = torch.empty_like(a)
+    aux = torch.empty_like(a)
+    torch.cuda.synchronize()
+
+    def step():
+        plan.execute(a, b, dt.Execute.FORWARD, aux)
+        plan.execute(b, a, dt.Execute.BACKWARD, aux)
+
+    # round-trip error (outside the timed region): fwd, bwd, scale
+    step()
+    torch.cuda.synchronize()
+    rt = float(torch.linalg.vector_norm(a / (DIMS[0] * DIMS[1] * DIMS[2]) - x0) / torch.linalg.vector_norm(x0))
+
+    for _ in range(args.warmup):
+        a.copy_(x0)
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = dt.kernel_launches()
+    L.dtfft_gb_profile_start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    L.dtfft_gb_profile_stop()
+    launches = dt.kernel_launches() - launches0
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    prof = _profile_results(L)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * 1000.0 / ms_step
+
+    # dominant kernel of the timed region
+    top = max(prof, key=lambda r: r[2]) if prof else ("none", 1, 0.0)
+    per_launch_ms = top[2] / max(top[1], 1)
+    algo_bytes = 2 * nbytes          # one read + one write of the whole buffer per launch
+    achieved = algo_bytes / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
+    peak, peak_kind = _peaks()
+    # unfused pass count of the generic schedule: 2 x (3 FFT + 2 transposes), each one read + one write
+    step_bytes = 2 * (3 + 2) * 2 * nbytes
+    eff_tbs = step_bytes / (ms_step * 1e-3) / 1e12
+
+    # e2e: host buffers through the C ABI; the host->device copy of the input and
+    # the device->host copy of the result are inside the timed region
+    e2e_ms = None
+    if not args.no_e2e:
+        host_in = torch.empty(n, dtype=torch.complex64, pin_memory=True)
+        host_in.copy_(x0.cpu())
+        host_out = torch.empty(n, dtype=torch.complex64, pin_memory=True)
+        e2e_steps = max(1, min(args.steps, 10))
+
+        def e2e_step():
+            a.copy_(host_in, non_blocking=True)
+            step()
+            host_out.copy_(a, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(e2e_steps):
+            e2e_step()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = f0.elapsed_time(f1) / e2e_steps
+        if world > 1:
+            t = torch.tensor([e2e_ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline()
+        except Exception as ex:  # report, never fake
+            cpu = {"value": None, "unit": "cycles/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {ex}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cycles/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "dims": DIMS, "grid": "1x2x4 virtual ranks", "precision": "single",
+                       "executor": "own Stockham kernels", "l2": "inputs larger than L2 (1 GiB per buffer)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "hbm_tbs_effective": eff_tbs,
+            "roundtrip_rel_l2": rt,
+            "roofline": {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": _traffic_for(top[0]), "algorithmic_bytes": algo_bytes,
+                         "launch_ms": per_launch_ms},
+            "kernels": [{"name": k, "launches": c, "total_ms": t} for k, c, t in sorted(prof, key=lambda r: -r[2])],
+            "e2e": ({"value": world * 1000.0 / e2e_ms, "unit": "cycles/s", "h2d_bytes_per_step": nbytes,
+                     "d2h_bytes_per_step": nbytes} if e2e_ms else None),
+            "gpu_launches": launches,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    plan.destroy()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--effort", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--dims", type=int, nargs=3, default=None,
+                    help="smaller C2C case for profiling (default: the 512^3 headline workload)")
+    ap.add_argument("--grid", type=int, nargs=2, default=[2, 4])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <string>
 #include <vector>
 
 #include "dtfft.h"
@@ -20,6 +21,11 @@ struct __align__(16) e16 { uint64_t lo, hi; };
 // Number of this library's kernel launches since load (benchmark accounting).
 extern std::atomic<int64_t> g_launches;
 inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Optional per-launch event timing (profile.cpp); prof_begin returns nullptr when off.
+void* prof_begin(cudaStream_t s);
+void prof_end(void* token, const std::string& name, cudaStream_t s);
+bool profiling();
 
 #define GB_CUDA_TRY(expr)                                             \
     do {                                                              \

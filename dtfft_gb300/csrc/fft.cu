@@ -386,6 +386,265 @@ __global__ void __launch_bounds__(256) fft_kernel(Args<R> A) {
     }
 }
 
+// ===========================================================================
+// Register-resident Stockham kernel (fast path)
+//
+// A signal of m points is owned by T = m / E threads; thread t keeps the E
+// points t + T*q (q < E) in registers.  With that ownership every radix-R
+// stage is local: butterfly j = t + b*T (b < E/R) reads points j + r*m/R =
+// t + T*(b + r*E/R), which the thread already holds.  Only the Stockham output
+// permutation between stages goes through shared memory (one write, one read
+// per point and stage boundary, padded i + i/16 against bank conflicts).  The
+// last stage's outputs land on points t + T*q again, so the first stage loads
+// and the last stage stores straight from / to HBM with the warp's lanes on
+// consecutive addresses.  Real-transform pre/post work is folded into those
+// global loads and stores; only R2C with even n exchanges once more.
+// ===========================================================================
+
+// W16^e = exp(s * 2*pi*i*e/16), e in [0, 9]
+template <typename R, typename C>
+__device__ __forceinline__ C w16(int e, int s) {
+    const R cs[10] = {(R)1, (R)0.92387953251128675613, (R)0.70710678118654752440, (R)0.38268343236508977173, (R)0,
+                      (R)-0.38268343236508977173, (R)-0.70710678118654752440, (R)-0.92387953251128675613, (R)-1,
+                      (R)-0.92387953251128675613};
+    const R sn[10] = {(R)0, (R)0.38268343236508977173, (R)0.70710678118654752440, (R)0.92387953251128675613, (R)1,
+                      (R)0.92387953251128675613, (R)0.70710678118654752440, (R)0.38268343236508977173, (R)0,
+                      (R)-0.38268343236508977173};
+    C w; w.x = cs[e]; w.y = s > 0 ? sn[e] : -sn[e];
+    return w;
+}
+
+template <typename R, typename C>
+__device__ __forceinline__ void dft16(C* v, int s) {
+    C a[4][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) a[q][r] = v[q + 4 * r];
+        dft4<R>(a[q], s);
+#pragma unroll
+        for (int k1 = 1; k1 < 4; ++k1)
+            if (q) a[q][k1] = cmul(a[q][k1], w16<R, C>(q * k1, s));
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+        C b[4] = {a[0][k1], a[1][k1], a[2][k1], a[3][k1]};
+        dft4<R>(b, s);
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = b[k2];
+    }
+}
+
+template <typename R, int RAD, typename C>
+__device__ __forceinline__ void dft_any(C* w, int s) {
+    if constexpr (RAD == 2) dft2<R>(w[0], w[1]);
+    else if constexpr (RAD == 3) dft3<R>(w, s);
+    else if constexpr (RAD == 4) dft4<R>(w, s);
+    else if constexpr (RAD == 5) dft5<R>(w, s);
+    else if constexpr (RAD == 7) dft7<R>(w, s);
+    else if constexpr (RAD == 8) dft8<R>(w, s);
+    else if constexpr (RAD == 16) dft16<R>(w, s);
+}
+
+__device__ __forceinline__ int rpad(int i) { return i + (i >> 4); }
+
+// smem slot of point i of local signal sl
+template <bool COLS>
+__device__ __forceinline__ int rslot(int sl, int i, int spitch, int S) {
+    return COLS ? i * S + sl : sl * spitch + rpad(i);
+}
+
+// One radix-RAD stage on the registers of thread t; with EX the outputs are
+// written to their Stockham positions in smem (the exchange).
+template <typename R, int E, int RAD, bool COLS, bool EX>
+__device__ __forceinline__ void reg_stage(typename CT<R>::T (&v)[E], int t, int T, int Ns, int m,
+                                          const typename CT<R>::T* __restrict__ tw, int s,
+                                          typename CT<R>::T* sm, int sl, int spitch, int S) {
+    typedef typename CT<R>::T C;
+    constexpr int B = E / RAD;
+    const int tstep = m / (Ns * RAD);
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = t + b * T;
+        const int k = j % Ns;
+        C w[RAD];
+#pragma unroll
+        for (int r = 0; r < RAD; ++r) w[r] = v[b + r * B];
+        if (k != 0) {
+            const int e1 = tstep * k;
+#pragma unroll
+            for (int r = 1; r < RAD; ++r) {
+                C tv = __ldg(&tw[e1 * r]);
+                if (s > 0) tv.y = -tv.y;
+                w[r] = cmul(w[r], tv);
+            }
+        }
+        dft_any<R, RAD>(w, s);
+        if constexpr (EX) {
+            const int base = (j - k) * RAD + k;
+#pragma unroll
+            for (int r = 0; r < RAD; ++r) sm[rslot<COLS>(sl, base + r * Ns, spitch, S)] = w[r];
+        } else {
+#pragma unroll
+            for (int r = 0; r < RAD; ++r) v[b + r * B] = w[r];
+        }
+    }
+}
+
+template <typename R, int E, bool COLS, bool EX>
+__device__ __forceinline__ bool reg_stage_any(int rad, typename CT<R>::T (&v)[E], int t, int T, int Ns, int m,
+                                              const typename CT<R>::T* tw, int s, typename CT<R>::T* sm, int sl,
+                                              int spitch, int S) {
+    switch (rad) {
+    case 2: if constexpr (E % 2 == 0) { reg_stage<R, E, 2, COLS, EX>(v, t, T, Ns, m, tw, s, sm, sl, spitch, S); return true; } break;
+    case 3: if constexpr (E % 3 == 0) { reg_stage<R, E, 3, COLS, EX>(v, t, T, Ns, m, tw, s, sm, sl, spitch, S); return true; } break;
+    case 4: if constexpr (E % 4 == 0) { reg_stage<R, E, 4, COLS, EX>(v, t, T, Ns, m, tw, s, sm, sl, spitch, S); return true; } break;
+    case 5: if constexpr (E % 5 == 0) { reg_stage<R, E, 5, COLS, EX>(v, t, T, Ns, m, tw, s, sm, sl, spitch, S); return true; } break;
+    case 7: if constexpr (E % 7 == 0) { reg_stage<R, E, 7, COLS, EX>(v, t, T, Ns, m, tw, s, sm, sl, spitch, S); return true; } break;
+    case 8: if constexpr (E % 8 == 0) { reg_stage<R, E, 8, COLS, EX>(v, t, T, Ns, m, tw, s, sm, sl, spitch, S); return true; } break;
+    case 16: if constexpr (E % 16 == 0) { reg_stage<R, E, 16, COLS, EX>(v, t, T, Ns, m, tw, s, sm, sl, spitch, S); return true; } break;
+    }
+    return false;
+}
+
+template <typename R, int E, bool COLS, bool C2C_ONLY>
+__global__ void __launch_bounds__(256) fft_reg_kernel(Args<R> A) {
+    typedef typename CT<R>::T C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* sm = reinterpret_cast<C*>(smem_raw);
+    const int S = A.per_cta;          // signals per CTA
+    const int T = A.m / E;            // threads per signal
+    int sl, t;
+    if (COLS) { sl = threadIdx.x % S; t = threadIdx.x / S; }
+    else { sl = threadIdx.x / T; t = threadIdx.x % T; }
+    const i64 sig = (i64)blockIdx.x * S + sl;
+    const bool live = sig < A.nsig;
+    const int n = A.n, m = A.m, s = A.sign, spitch = A.pitch;
+    const int mode = C2C_ONLY ? (int)M_C2C : A.mode;
+    const C* inC = reinterpret_cast<const C*>(A.in);
+    const R* inR = reinterpret_cast<const R*>(A.in);
+    C* outC = reinterpret_cast<C*>(A.out);
+    R* outR = reinterpret_cast<R*>(A.out);
+
+    // ---- load core input points i = t + T*q ----
+    C v[E];
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+        const int i = t + T * q;
+        C x; x.x = 0; x.y = 0;
+        if (live) {
+            switch (mode) {
+            case M_C2C: x = inC[gin<R, COLS>(A, sig, i)]; break;
+            case M_R2C_HALF: x = *reinterpret_cast<const C*>(inR + gin<R, COLS>(A, sig, 2 * i)); break;
+            case M_R2C_FULL: x.x = inR[gin<R, COLS>(A, sig, i)]; break;
+            case M_C2R_HALF: {
+                C xk = inC[gin<R, COLS>(A, sig, i)];
+                C xm = inC[gin<R, COLS>(A, sig, m - i)];
+                if (i == 0) { xk.y = 0; xm.y = 0; }
+                C cxm = cconj(xm);
+                C o = cmul(csub(xk, cxm), cconj(__ldg(&A.ta[i])));
+                x = cadd(cadd(xk, cxm), cmul_is(o, 1));
+            } break;
+            case M_C2R_FULL:
+                if (i <= n / 2) { x = inC[gin<R, COLS>(A, sig, i)]; if (i == 0) x.y = 0; }
+                else x = cconj(inC[gin<R, COLS>(A, sig, n - i)]);
+                break;
+            case M_DCT1: x.x = inR[gin<R, COLS>(A, sig, i < n ? i : m - i)]; break;
+            case M_DST1:
+                if (i >= 1 && i <= n) x.x = inR[gin<R, COLS>(A, sig, i - 1)];
+                else if (i >= n + 2) x.x = -inR[gin<R, COLS>(A, sig, m - i - 1)];
+                break;
+            case M_DCT2: case M_DST2: {
+                const int j = (2 * i < n) ? 2 * i : 2 * (n - 1 - i) + 1;
+                R y = inR[gin<R, COLS>(A, sig, j)];
+                if (mode == M_DST2 && (j & 1)) y = -y;
+                x.x = y;
+            } break;
+            case M_DCT3: case M_DST3: {
+                R a, b = 0;
+                if (mode == M_DCT3) { a = inR[gin<R, COLS>(A, sig, i)]; if (i > 0) b = inR[gin<R, COLS>(A, sig, n - i)]; }
+                else { a = inR[gin<R, COLS>(A, sig, n - 1 - i)]; if (i > 0) b = inR[gin<R, COLS>(A, sig, i - 1)]; }
+                C tt; tt.x = a; tt.y = -b;
+                x = cmul(tt, cconj(__ldg(&A.ta[i])));
+            } break;
+            case M_DCT4: case M_DST4:
+                if (i < n) {
+                    C tt; tt.x = inR[gin<R, COLS>(A, sig, mode == M_DCT4 ? i : n - 1 - i)]; tt.y = 0;
+                    x = cmul(tt, __ldg(&A.ta[i]));
+                }
+                break;
+            }
+        }
+        v[q] = x;
+    }
+    // every point of the CTA is read before any is written (in-place safety)
+    __syncthreads();
+
+    // ---- stages ----
+    int Ns = 1;
+    const int ns = A.st.ns;
+    for (int st = 0; st < ns - 1; ++st) {
+        const int rad = A.st.radix[st];
+        reg_stage_any<R, E, COLS, true>(rad, v, t, T, Ns, m, A.tw, s, sm, sl, spitch, S);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < E; ++q) v[q] = sm[rslot<COLS>(sl, t + T * q, spitch, S)];
+        __syncthreads();
+        Ns *= rad;
+    }
+    if (ns > 0) reg_stage_any<R, E, COLS, false>(A.st.radix[ns - 1], v, t, T, Ns, m, A.tw, s, sm, sl, spitch, S);
+
+    // ---- store core output points i = t + T*q ----
+    if (mode == M_R2C_HALF) {
+        // X[k] needs Z[k] and Z[m-k]: one more exchange
+#pragma unroll
+        for (int q = 0; q < E; ++q) sm[rslot<COLS>(sl, t + T * q, spitch, S)] = v[q];
+        __syncthreads();
+        if (live) {
+            for (int k = t; k <= m; k += T) {
+                C zk = sm[rslot<COLS>(sl, k == m ? 0 : k, spitch, S)];
+                C zm = cconj(sm[rslot<COLS>(sl, k == 0 ? 0 : m - k, spitch, S)]);
+                C e = cscale(cadd(zk, zm), (R)0.5);
+                C o = cscale(csub(zk, zm), (R)0.5);
+                C tt = cmul(__ldg(&A.ta[k]), o);
+                outC[gout<R, COLS>(A, sig, k)] = cadd(e, cmul_is(tt, -1));
+            }
+        }
+        return;
+    }
+    if (!live) return;
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+        const int i = t + T * q;
+        const C f = v[q];
+        switch (mode) {
+        case M_C2C: outC[gout<R, COLS>(A, sig, i)] = f; break;
+        case M_R2C_FULL: if (i <= n / 2) outC[gout<R, COLS>(A, sig, i)] = f; break;
+        case M_C2R_HALF: *reinterpret_cast<C*>(outR + gout<R, COLS>(A, sig, 2 * i)) = f; break;
+        case M_C2R_FULL: outR[gout<R, COLS>(A, sig, i)] = f.x; break;
+        case M_DCT1: if (i < n) outR[gout<R, COLS>(A, sig, i)] = f.x; break;
+        case M_DST1: if (i >= 1 && i <= n) outR[gout<R, COLS>(A, sig, i - 1)] = -f.y; break;
+        case M_DCT2: case M_DST2: {
+            C w = __ldg(&A.ta[i]);
+            R y = (R)2 * (w.x * f.x - w.y * f.y);
+            outR[gout<R, COLS>(A, sig, mode == M_DCT2 ? i : n - 1 - i)] = y;
+        } break;
+        case M_DCT3: case M_DST3: {
+            if (2 * i < n) outR[gout<R, COLS>(A, sig, 2 * i)] = f.x;
+            const int k2 = 2 * (n - 1 - i) + 1;
+            if (k2 < n) outR[gout<R, COLS>(A, sig, k2)] = mode == M_DST3 ? -f.x : f.x;
+        } break;
+        case M_DCT4: case M_DST4: {
+            if (i >= n) break;
+            C w = __ldg(&A.tb[i]);
+            R y = (R)2 * (w.x * f.x - w.y * f.y);
+            if (mode == M_DST4 && (i & 1)) y = -y;
+            outR[gout<R, COLS>(A, sig, i)] = y;
+        } break;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
@@ -428,8 +687,44 @@ struct FftStep {
     const void* tb = nullptr;
     Schedule sched;
     size_t smem = 0;
+    int E = 0;               // points per thread of the register kernel, 0 = shared-memory kernel
+    int threads = 256;
     bool reads_out = false;  // step reads the plan's output buffer (second pass)
 };
+
+// Register-kernel schedule: points per thread E (compiled: 8, 16, 24, 20, 28),
+// radices dividing E, fewest stages first, then fewest registers.
+static bool make_reg_schedule(int m, bool cols, int& E_out, Schedule& sch, int& T_out) {
+    static const int Es[] = {8, 16, 24, 20, 28};
+    static const int rads[] = {16, 8, 7, 5, 4, 3, 2};
+    int best_stages = 1 << 30, best_E = 0;
+    Schedule best;
+    for (int E : Es) {
+        if (m % E != 0) continue;
+        const int T = m / E;
+        if (T < 1 || T > 256) continue;
+        if (cols && T > 64) continue;
+        Schedule s;
+        s.m = m;
+        int r = m;
+        while (r > 1) {
+            int pick = 0;
+            for (int q : rads)
+                if (E % q == 0 && r % q == 0) { pick = q; break; }
+            if (!pick) break;
+            s.radix.push_back(pick);
+            r /= pick;
+        }
+        if (r != 1) continue;
+        const int st = (int)s.radix.size();
+        if (st < best_stages || (st == best_stages && E < best_E)) { best_stages = st; best_E = E; best = s; }
+    }
+    if (!best_E) return false;
+    E_out = best_E;
+    T_out = m / best_E;
+    sch = best;
+    return true;
+}
 
 static int mode_for_r2r(int kind) {
     switch (kind) {
@@ -512,8 +807,20 @@ static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
     if (!mode_geometry(S.mode, S.n, S.sign, m, sign)) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     S.m = m;
     S.sign = sign;
-    if (!make_schedule(m, S.sched)) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     const size_t es = S.dbl ? 16 : 8;
+    int E = 0, T = 0;
+    if (!getenv("DTFFT_GB_NO_REG_FFT") && make_reg_schedule(m, S.cols, E, S.sched, T)) {
+        S.E = E;
+        // S signals per CTA, blockDim = S*T (signals past the end are masked)
+        S.per = std::max(1, 256 / T);
+        S.threads = S.per * T;
+        S.pitch = m + m / 16;
+        S.smem = S.cols ? (size_t)m * S.per * es : (size_t)S.per * S.pitch * es;
+    } else if (!make_schedule(m, S.sched)) {
+        return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    }
+    if (S.E) goto tables;
+    {
     const size_t per_sig = 2 * (size_t)m * es;   // ping-pong buffers
     if (per_sig > 220 * 1024) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     int per;
@@ -532,6 +839,8 @@ static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
     }
     S.per = std::max(1, per);
     S.smem = (size_t)S.per * per_sig;
+    }
+tables:
     // tables
     std::vector<double> tw = table_exp(m, 1, m);
     GB_TRY(upload_table(tw, S.dbl, owned, &S.tw));
@@ -569,9 +878,32 @@ static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, 
     const i64 ctas = (S.nsig + S.per - 1) / S.per;
     if (ctas <= 0) return DTFFT_SUCCESS;
     if (ctas > 0x7fffffffLL) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-    if (S.smem > 48 * 1024)
-        GB_CUDA_TRY(cudaFuncSetAttribute(fft_kernel<R, COLS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
-    fft_kernel<R, COLS><<<(unsigned)ctas, 256, S.smem, s>>>(A);
+    void* tok = prof_begin(s);
+    if (S.E) {
+        void (*kfn)(Args<R>) = nullptr;
+        const bool c2c = S.mode == M_C2C;
+        switch (S.E) {
+        case 8: kfn = c2c ? fft_reg_kernel<R, 8, COLS, true> : fft_reg_kernel<R, 8, COLS, false>; break;
+        case 16: kfn = c2c ? fft_reg_kernel<R, 16, COLS, true> : fft_reg_kernel<R, 16, COLS, false>; break;
+        case 24: kfn = c2c ? fft_reg_kernel<R, 24, COLS, true> : fft_reg_kernel<R, 24, COLS, false>; break;
+        case 20: kfn = c2c ? fft_reg_kernel<R, 20, COLS, true> : fft_reg_kernel<R, 20, COLS, false>; break;
+        case 28: kfn = c2c ? fft_reg_kernel<R, 28, COLS, true> : fft_reg_kernel<R, 28, COLS, false>; break;
+        default: return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+        }
+        if (S.smem > 48 * 1024)
+            GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
+        kfn<<<(unsigned)ctas, S.threads, S.smem, s>>>(A);
+    } else {
+        if (S.smem > 48 * 1024)
+            GB_CUDA_TRY(cudaFuncSetAttribute(fft_kernel<R, COLS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
+        fft_kernel<R, COLS><<<(unsigned)ctas, 256, S.smem, s>>>(A);
+    }
+    if (tok) {
+        static const char* mn[] = {"c2c", "r2c", "r2c", "c2r", "c2r", "dct1", "dct2", "dct3", "dct4",
+                                   "dst1", "dst2", "dst3", "dst4"};
+        prof_end(tok, std::string(S.E ? "fftreg_" : "fft_") + (COLS ? "cols_" : "rows_") + mn[S.mode] + "_m" +
+                          std::to_string(S.m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
+    }
     count_launch();
     GB_CUDA_TRY(cudaGetLastError());
     return DTFFT_SUCCESS;
@@ -638,6 +970,9 @@ dtfft_error_t FftPlan::build(int sign, std::vector<FftStep*>& steps) {
     } break;
     default: delete row; return DTFFT_ERROR_INVALID_USAGE;
     }
+    // rank 1: idist/odist describe the forward (real -> complex) direction;
+    // the C2R step reads complex rows odist apart and writes real rows idist apart
+    if (d.rank == 1 && d.type == FFT_R2C && sign == FFT_BWD) std::swap(in_row, out_row);
     row->idist = in_row; row->odist = out_row;
     dtfft_error_t e = prepare_step(*row, tables_);
     if (e != DTFFT_SUCCESS) { delete row; return e; }

@@ -157,6 +157,7 @@ static bool launch_cfg(const BoxList& bl, const void* in, void* out, cudaStream_
 
 dtfft_error_t boxes_launch(const BoxList& bl, const void* in, void* out, cudaStream_t stream) {
     if (bl.total_tiles == 0) return DTFFT_SUCCESS;
+    void* tok = prof_begin(stream);
     bool ok = false;
     switch (bl.elem) {
     case 4: ok = launch_cfg<uint32_t>(bl, in, out, stream); break;
@@ -165,6 +166,11 @@ dtfft_error_t boxes_launch(const BoxList& bl, const void* in, void* out, cudaStr
     default: return DTFFT_ERROR_INVALID_USAGE;
     }
     if (!ok) return DTFFT_ERROR_INVALID_USAGE;
+    if (tok) {
+        std::string nm = std::string(bl.copy ? "copy" : "transpose") + "_e" + std::to_string(bl.elem) + "_t" +
+                         std::to_string(bl.cfg.tile_a) + "x" + std::to_string(bl.cfg.tile_b);
+        prof_end(tok, nm, stream);
+    }
     count_launch();
     GB_CUDA_TRY(cudaGetLastError());
     return DTFFT_SUCCESS;

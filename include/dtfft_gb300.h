@@ -134,6 +134,16 @@ dtfft_error_t dtfft_vgrid_get_pencil(dtfft_plan_t plan, dtfft_layout_t layout, i
 /** Number of launches of this library's kernels since load (for benchmarks). */
 int64_t dtfft_gb_kernel_launch_count(void);
 
+/* ------------------------------------------------------------------------ */
+/* Kernel timing (for benchmarks)                                            */
+/* Between start and stop every launch is bracketed by CUDA events on its    */
+/* stream; durations are summed per kernel name.                             */
+/* ------------------------------------------------------------------------ */
+void dtfft_gb_profile_start(void);
+void dtfft_gb_profile_stop(void);
+int32_t dtfft_gb_profile_count(void);
+int32_t dtfft_gb_profile_get(int32_t index, char* name, int32_t name_len, int64_t* launches, double* total_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,6 +17,8 @@ def to_dev(a: np.ndarray, n_alloc: int, dev):
     t = torch.zeros(max(n_alloc, a.size), dtype=torch_dtype(a.dtype), device=dev)
     if a.size:
         t[: a.size] = torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    # plans run on their own stream: finish torch's work before handing buffers over
+    torch.cuda.synchronize()
     return t
 
 
@@ -34,6 +36,7 @@ def empty(n_alloc: int, np_dtype, dev, fill=np.nan):
         t.imag.fill_(fill)
     else:
         t.fill_(fill)
+    torch.cuda.synchronize()
     return t
 
 
