@@ -56,6 +56,7 @@ struct Box {
     i64 src_off, dst_off;
     int32_t na, nb, nc;
     int32_t tiles_a, tiles_b;   // tiles per c-plane (set by the launcher)
+    int32_t a0;                 // start of the box along the source block's contiguous axis
     i64 sb, sc;                 // source strides of b and c
     i64 da_or_db, dc;           // destination stride of a (transpose) or b (copy), and of c
     i64 tile_begin;             // first global tile index of this box

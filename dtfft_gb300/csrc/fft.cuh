@@ -59,4 +59,27 @@ private:
     dtfft_error_t twiddles(int m, const void** table);
 };
 
+// Batched C2C along the source layout's aligned axis fused with the transpose
+// described by a box list: one HBM pass instead of two.
+class FusedFT {
+public:
+    // Fails (without side effects) when the boxes do not give every source
+    // rank whole rows of the transform axis or the length has no register schedule.
+    static dtfft_error_t create(const BoxList& bl, int m, int dbl, FusedFT** out);
+    ~FusedFT();
+    dtfft_error_t execute(const void* in, void* out, int sign, cudaStream_t s);
+
+private:
+    int m_ = 0, dbl_ = 0, E_ = 0, T_ = 0, S_ = 1, pitch_ = 0, ngroups_ = 0;
+    i64 ctas_ = 0;
+    size_t smem_ = 0;
+    size_t pipe_smem_ = 0;   // TMA-pipelined persistent variant (0 CTAs/SM = not used)
+    int pipe_per_sm_ = 0;
+    Schedule sched_;
+    const void* tw_ = nullptr;
+    const void* groups_ = nullptr;
+    const void* segs_ = nullptr;
+    std::vector<void*> owned_;
+};
+
 }  // namespace gb

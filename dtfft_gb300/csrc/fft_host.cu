@@ -1,0 +1,618 @@
+// Host side of the FFT executor: schedules, twiddle tables, launch shapes,
+// and the fused FFT + transpose steps.  Kernels live in fft_kernels.cuh.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <sstream>
+
+#include "fft_kernels.cuh"
+
+namespace gb {
+
+// Device status word written by the pipelined kernels when a bounded wait gives up.
+__device__ int g_gb_status = 0;
+
+static int* status_ptr() {
+    static int* p = nullptr;
+    if (!p && cudaGetSymbolAddress((void**)&p, g_gb_status) != cudaSuccess) { cudaGetLastError(); p = nullptr; }
+    return p;
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+std::string Schedule::str() const {
+    std::ostringstream o;
+    for (size_t i = 0; i < radix.size(); ++i) o << (i ? "x" : "") << radix[i];
+    return o.str();
+}
+
+bool make_schedule(int m, Schedule& s) {
+    s.m = m;
+    s.radix.clear();
+    int r = m;
+    while (r % 8 == 0) { s.radix.push_back(8); r /= 8; }
+    if (r % 4 == 0) { s.radix.push_back(4); r /= 4; }
+    if (r % 2 == 0) { s.radix.push_back(2); r /= 2; }
+    const int small[] = {3, 5, 7};
+    for (int p : small) while (r % p == 0) { s.radix.push_back(p); r /= p; }
+    for (int p = 11; p <= 127 && r > 1; p += 2) {
+        bool prime = true;
+        for (int q = 3; q * q <= p; q += 2) if (p % q == 0) { prime = false; break; }
+        if (!prime) continue;
+        while (r % p == 0) { s.radix.push_back(p); r /= p; }
+    }
+    if (r != 1) return false;
+    if (s.radix.size() > 26) return false;
+    return true;
+}
+
+struct FftStep {
+    bool cols = false;
+    int dbl = 0;
+    int mode = M_C2C;
+    int sign = -1;
+    // geometry
+    i64 nsig = 0, idist = 0, odist = 0, plane = 0;
+    int ld = 0, ncols = 0, n = 0, m = 0, per = 1, pitch = 0;
+    const void* tw = nullptr;
+    const void* ta = nullptr;
+    const void* tb = nullptr;
+    Schedule sched;
+    size_t smem = 0;
+    int E = 0;               // points per thread of the register kernel, 0 = shared-memory kernel
+    int threads = 256;
+    bool pipe = false;       // C2C rows: persistent TMA-pipelined kernel when buffers are 16-byte aligned
+    size_t pipe_smem = 0;
+    int pipe_ctas_per_sm = 0;
+    bool reads_out = false;  // step reads the plan's output buffer (second pass)
+};
+
+// Register-kernel schedule: points per thread E (compiled: 8, 16, 24, 20, 28),
+// radices dividing E, fewest stages first, then fewest registers.
+static bool make_reg_schedule(int m, bool cols, int& E_out, Schedule& sch, int& T_out, int max_T = 256) {
+    static const int Es[] = {8, 16, 24, 20, 28};
+    static const int rads[] = {16, 8, 7, 5, 4, 3, 2};
+    int best_stages = 1 << 30, best_E = 0;
+    Schedule best;
+    for (int E : Es) {
+        if (m % E != 0) continue;
+        const int T = m / E;
+        if (T < 1 || T > max_T) continue;
+        if (cols && T > 64) continue;
+        Schedule s;
+        s.m = m;
+        int r = m;
+        while (r > 1) {
+            int pick = 0;
+            for (int q : rads)
+                if (E % q == 0 && r % q == 0) { pick = q; break; }
+            if (!pick) break;
+            s.radix.push_back(pick);
+            r /= pick;
+        }
+        if (r != 1) continue;
+        const int st = (int)s.radix.size();
+        if (st < best_stages || (st == best_stages && E < best_E)) { best_stages = st; best_E = E; best = s; }
+    }
+    if (!best_E) return false;
+    E_out = best_E;
+    T_out = m / best_E;
+    sch = best;
+    return true;
+}
+
+static int mode_for_r2r(int kind) {
+    switch (kind) {
+    case DTFFT_DCT_1: return M_DCT1;
+    case DTFFT_DCT_2: return M_DCT2;
+    case DTFFT_DCT_3: return M_DCT3;
+    case DTFFT_DCT_4: return M_DCT4;
+    case DTFFT_DST_1: return M_DST1;
+    case DTFFT_DST_2: return M_DST2;
+    case DTFFT_DST_3: return M_DST3;
+    case DTFFT_DST_4: return M_DST4;
+    }
+    return -1;
+}
+
+static int inverse_kind(int kind) {  // src/dtfft_utils.F90:447-471
+    switch (kind) {
+    case DTFFT_DCT_2: return DTFFT_DCT_3;
+    case DTFFT_DCT_3: return DTFFT_DCT_2;
+    case DTFFT_DST_2: return DTFFT_DST_3;
+    case DTFFT_DST_3: return DTFFT_DST_2;
+    default: return kind;
+    }
+}
+
+// Core length and core sign of a mode for a signal of logical length n.
+static bool mode_geometry(int mode, int n, int plan_sign, int& m, int& sign) {
+    sign = plan_sign;
+    switch (mode) {
+    case M_C2C: m = n; break;
+    case M_R2C_HALF: m = n / 2; sign = -1; break;
+    case M_R2C_FULL: m = n; sign = -1; break;
+    case M_C2R_HALF: m = n / 2; sign = 1; break;
+    case M_C2R_FULL: m = n; sign = 1; break;
+    case M_DCT1: if (n < 2) return false; m = 2 * (n - 1); sign = -1; break;
+    case M_DST1: m = 2 * (n + 1); sign = -1; break;
+    case M_DCT2: case M_DST2: m = n; sign = -1; break;
+    case M_DCT3: case M_DST3: m = n; sign = 1; break;
+    case M_DCT4: case M_DST4: m = 2 * n; sign = -1; break;
+    default: return false;
+    }
+    return m >= 1;
+}
+
+// Host table of exp(-2*pi*i*j*num/den) for j < count, built in double precision.
+static std::vector<double> table_exp(int count, long long num, long long den) {
+    std::vector<double> t(2 * (size_t)count);
+    for (int j = 0; j < count; ++j) {
+        // reduce j*num mod den exactly before converting to an angle
+        long long q = ((long long)j * num) % den;
+        double ang = -2.0 * M_PI * (double)q / (double)den;
+        t[2 * j] = std::cos(ang);
+        t[2 * j + 1] = std::sin(ang);
+    }
+    return t;
+}
+
+static dtfft_error_t upload_table(const std::vector<double>& t, int dbl, std::vector<void*>& owned, const void** out) {
+    size_t n = t.size();
+    void* d = nullptr;
+    if (dbl) {
+        GB_CUDA_TRY(cudaMalloc(&d, n * sizeof(double)));
+        GB_CUDA_TRY(cudaMemcpy(d, t.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> f(n);
+        for (size_t i = 0; i < n; ++i) f[i] = (float)t[i];
+        GB_CUDA_TRY(cudaMalloc(&d, n * sizeof(float)));
+        GB_CUDA_TRY(cudaMemcpy(d, f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    owned.push_back(d);
+    *out = d;
+    return DTFFT_SUCCESS;
+}
+
+static const size_t kSmemBudget = 96 * 1024;
+
+// Fill geometry, tables and launch shape of one step.
+static int pipe_occupancy(int dbl, int m, int E, bool fused, int threads, size_t smem);
+
+static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
+    int m, sign;
+    if (!mode_geometry(S.mode, S.n, S.sign, m, sign)) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    S.m = m;
+    S.sign = sign;
+    const size_t es = S.dbl ? 16 : 8;
+    int E = 0, T = 0;
+    if (!getenv("DTFFT_GB_NO_REG_FFT") && make_reg_schedule(m, S.cols, E, S.sched, T)) {
+        S.E = E;
+        // S signals per CTA, blockDim = S*T (signals past the end are masked)
+        S.per = std::max(1, 256 / T);
+        S.threads = S.per * T;
+        S.pitch = m + m / 16;
+        S.smem = S.cols ? (size_t)m * S.per * es : (size_t)S.per * S.pitch * es;
+        // contiguous C2C rows stream through the TMA pipeline (2 buffers in flight)
+        if (!S.cols && S.mode == M_C2C && S.idist == m && S.odist == m && (m * es) % 16 == 0 &&
+            !getenv("DTFFT_GB_NO_PIPE")) {
+            S.pipe_smem = 128 + 2 * (size_t)S.per * m * es + S.smem;
+            S.pipe_ctas_per_sm = pipe_occupancy(S.dbl, S.m, S.E, false, S.threads, S.pipe_smem);
+            S.pipe = S.pipe_ctas_per_sm > 0;
+        }
+    } else if (!make_schedule(m, S.sched)) {
+        return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    }
+    if (S.E) goto tables;
+    {
+    const size_t per_sig = 2 * (size_t)m * es;   // ping-pong buffers
+    if (per_sig > 220 * 1024) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    int per;
+    if (S.cols) {
+        per = S.dbl ? 8 : 16;
+        while (per > 1 && per * per_sig > 200 * 1024) per >>= 1;
+        per = std::min<i64>(per, S.ncols);
+        S.pitch = per;
+    } else {
+        per = (int)std::max<size_t>(1, kSmemBudget / per_sig);
+        // keep at least ~2 CTAs per SM worth of work when the batch is small
+        i64 want = std::max<i64>(1, S.nsig / (152 * 4));
+        per = (int)std::max<i64>(1, std::min<i64>(per, want));
+        per = std::min(per, 64);
+        S.pitch = m;
+    }
+    S.per = std::max(1, per);
+    S.smem = (size_t)S.per * per_sig;
+    }
+tables:
+    // tables
+    std::vector<double> tw = table_exp(m, 1, m);
+    GB_TRY(upload_table(tw, S.dbl, owned, &S.tw));
+    switch (S.mode) {
+    case M_R2C_HALF: GB_TRY(upload_table(table_exp(m + 1, 1, S.n), S.dbl, owned, &S.ta)); break;
+    case M_C2R_HALF: GB_TRY(upload_table(table_exp(m, 1, S.n), S.dbl, owned, &S.ta)); break;
+    case M_DCT2: case M_DST2: case M_DCT3: case M_DST3:
+        GB_TRY(upload_table(table_exp(S.n, 1, 4LL * S.n), S.dbl, owned, &S.ta)); break;
+    case M_DCT4: case M_DST4: {
+        GB_TRY(upload_table(table_exp(S.n, 1, 4LL * S.n), S.dbl, owned, &S.ta));
+        std::vector<double> t(2 * (size_t)S.n);
+        for (int k = 0; k < S.n; ++k) {
+            long long q = (2LL * k + 1) % (8LL * S.n);
+            double ang = -2.0 * M_PI * (double)q / (8.0 * S.n);
+            t[2 * k] = std::cos(ang); t[2 * k + 1] = std::sin(ang);
+        }
+        GB_TRY(upload_table(t, S.dbl, owned, &S.tb));
+    } break;
+    default: break;
+    }
+    return DTFFT_SUCCESS;
+}
+
+template <typename R, bool FUSED>
+static void (*pipe_fn(int m, int E))(PArgs<R>) {
+    return (void (*)(PArgs<R>))KPtr<R>::pipe(m, E, FUSED);
+}
+
+// CTAs of the pipelined kernel that fit one SM (0 when it cannot launch).
+static int pipe_occupancy(int dbl, int m, int E, bool fused, int threads, size_t smem) {
+    int n = 0;
+    auto one = [&](auto fn) {
+        if (!fn) return;
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
+        cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess) n = 0;
+    };
+    if (dbl) { if (fused) one(pipe_fn<double, true>(m, E)); else one(pipe_fn<double, false>(m, E)); }
+    else { if (fused) one(pipe_fn<float, true>(m, E)); else one(pipe_fn<float, false>(m, E)); }
+    cudaGetLastError();
+    return n;
+}
+
+static int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <typename R, bool FUSED>
+static dtfft_error_t launch_pipe(const PArgs<R>& P, int E, int threads, size_t smem, int per_sm, cudaStream_t s) {
+    void (*kfn)(PArgs<R>) = pipe_fn<R, FUSED>(P.m, E);
+    if (!kfn || per_sm <= 0) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    const i64 grid = std::min<i64>(P.ntiles, (i64)sm_count() * per_sm);
+    const_cast<PArgs<R>&>(P).status = status_ptr();
+    if (grid <= 0) return DTFFT_SUCCESS;
+    kfn<<<(unsigned)grid, threads, smem, s>>>(P);
+    return DTFFT_SUCCESS;
+}
+
+template <typename R, bool COLS>
+static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, cudaStream_t s) {
+    Args<R> A;
+    typedef typename CT<R>::T C;
+    if (!COLS && S.pipe && S.pipe_ctas_per_sm > 0 && ((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
+        PArgs<R> P;
+        P.in = (const C*)in; P.out = (C*)out;
+        P.nsig = S.nsig; P.groups = nullptr; P.segs = nullptr; P.ngroups = 0;
+        P.ntiles = (S.nsig + S.per - 1) / S.per;
+        P.m = S.m; P.sign = S.sign; P.S = S.per; P.pitch = S.pitch; P.nst = 2; P.tw = (const C*)S.tw;
+        P.st.ns = (int)S.sched.radix.size();
+        for (int i = 0; i < P.st.ns; ++i) P.st.radix[i] = S.sched.radix[i];
+        void* tok = prof_begin(s);
+        GB_TRY((launch_pipe<R, false>(P, S.E, S.threads, S.pipe_smem, S.pipe_ctas_per_sm, s)));
+        if (tok) prof_end(tok, std::string("fftpipe_rows_c2c_m") + std::to_string(S.m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
+        count_launch();
+        GB_CUDA_TRY(cudaGetLastError());
+        return DTFFT_SUCCESS;
+    }
+    A.in = (const char*)in; A.out = (char*)out;
+    A.nsig = S.nsig; A.idist = S.idist; A.odist = S.odist; A.plane = S.plane;
+    A.ld = S.ld; A.ncols = S.ncols; A.n = S.n; A.m = S.m; A.mode = S.mode; A.sign = S.sign;
+    A.per_cta = S.per; A.pitch = S.pitch;
+    A.tw = (const C*)S.tw; A.ta = (const C*)S.ta; A.tb = (const C*)S.tb;
+    A.st.ns = (int)S.sched.radix.size();
+    for (int i = 0; i < A.st.ns; ++i) A.st.radix[i] = S.sched.radix[i];
+    const i64 ctas = (S.nsig + S.per - 1) / S.per;
+    if (ctas <= 0) return DTFFT_SUCCESS;
+    if (ctas > 0x7fffffffLL) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    void* tok = prof_begin(s);
+    if (S.E) {
+        const bool c2c = S.mode == M_C2C;
+        void (*kfn)(Args<R>) = (void (*)(Args<R>))KPtr<R>::reg(S.E, COLS, c2c);
+        if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+        if (S.smem > 48 * 1024)
+            GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
+        // favour shared memory over L1 so several CTAs fit per SM
+        GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared));
+        kfn<<<(unsigned)ctas, S.threads, S.smem, s>>>(A);
+    } else {
+        void (*gfn)(Args<R>) = (void (*)(Args<R>))KPtr<R>::generic(COLS);
+        if (S.smem > 48 * 1024)
+            GB_CUDA_TRY(cudaFuncSetAttribute(gfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
+        gfn<<<(unsigned)ctas, 256, S.smem, s>>>(A);
+    }
+    if (tok) {
+        static const char* mn[] = {"c2c", "r2c", "r2c", "c2r", "c2r", "dct1", "dct2", "dct3", "dct4",
+                                   "dst1", "dst2", "dst3", "dst4"};
+        prof_end(tok, std::string(S.E ? "fftreg_" : "fft_") + (COLS ? "cols_" : "rows_") + mn[S.mode] + "_m" +
+                          std::to_string(S.m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
+    }
+    count_launch();
+    GB_CUDA_TRY(cudaGetLastError());
+    return DTFFT_SUCCESS;
+}
+
+static dtfft_error_t launch_step(const FftStep& S, const void* in, void* out, cudaStream_t s) {
+    if (S.dbl) return S.cols ? launch_step_t<double, true>(S, in, out, s) : launch_step_t<double, false>(S, in, out, s);
+    return S.cols ? launch_step_t<float, true>(S, in, out, s) : launch_step_t<float, false>(S, in, out, s);
+}
+
+dtfft_error_t FftPlan::create(const FftDesc& d, FftPlan** out) {
+    *out = nullptr;
+    if (d.rank != 1 && d.rank != 2) return DTFFT_ERROR_INVALID_USAGE;
+    if (d.n_fast < 1 || d.n_slow < 1 || d.batch < 0) return DTFFT_ERROR_INVALID_DIMENSION_SIZE;
+    FftPlan* p = new FftPlan();
+    p->d_ = d;
+    dtfft_error_t e = p->build(FFT_FWD, p->fwd_);
+    if (e == DTFFT_SUCCESS) e = p->build(FFT_BWD, p->bwd_);
+    if (e != DTFFT_SUCCESS) { delete p; return e; }
+    p->launches_ = (int)p->fwd_.size();
+    *out = p;
+    return DTFFT_SUCCESS;
+}
+
+FftPlan::~FftPlan() {
+    for (auto* s : fwd_) delete s;
+    for (auto* s : bwd_) delete s;
+    for (void* t : tables_) cudaFree(t);
+}
+
+// Steps of one direction:
+//   rank 1: one row step (any mode)
+//   rank 2: row step along n_fast, then an in-place column step along n_slow
+//           (C2R runs the column step first, on the input, then the row step)
+dtfft_error_t FftPlan::build(int sign, std::vector<FftStep*>& steps) {
+    const FftDesc& d = d_;
+    const int nf = d.n_fast, ns = d.n_slow;
+    const i64 planes = d.batch;
+    // row step
+    FftStep* row = new FftStep();
+    row->dbl = d.dbl; row->cols = false; row->sign = sign; row->n = nf;
+    row->nsig = planes * (d.rank == 2 ? ns : 1);
+    int row_ld_out = nf;  // complex row length after the row step (for the column step)
+    i64 in_row = d.rank == 2 ? 0 : d.idist, out_row = d.rank == 2 ? 0 : d.odist;
+    switch (d.type) {
+    case FFT_C2C:
+        row->mode = M_C2C;
+        if (d.rank == 2) { in_row = nf; out_row = nf; }
+        break;
+    case FFT_R2C:
+        if (sign == FFT_FWD) row->mode = (nf % 2 == 0) ? M_R2C_HALF : M_R2C_FULL;
+        else row->mode = (nf % 2 == 0) ? M_C2R_HALF : M_C2R_FULL;
+        row_ld_out = nf / 2 + 1;
+        if (d.rank == 2) {
+            if (sign == FFT_FWD) { in_row = nf; out_row = nf / 2 + 1; }
+            else { in_row = nf / 2 + 1; out_row = nf; }
+        }
+        break;
+    case FFT_R2R: {
+        int kind = sign == FFT_FWD ? d.kind_fast : inverse_kind(d.kind_fast);
+        row->mode = mode_for_r2r(kind);
+        if (row->mode < 0) { delete row; return DTFFT_ERROR_INVALID_R2R_KINDS; }
+        if (d.rank == 2) { in_row = nf; out_row = nf; }
+    } break;
+    default: delete row; return DTFFT_ERROR_INVALID_USAGE;
+    }
+    // rank 1: idist/odist describe the forward (real -> complex) direction;
+    // the C2R step reads complex rows odist apart and writes real rows idist apart
+    if (d.rank == 1 && d.type == FFT_R2C && sign == FFT_BWD) std::swap(in_row, out_row);
+    row->idist = in_row; row->odist = out_row;
+    dtfft_error_t e = prepare_step(*row, tables_);
+    if (e != DTFFT_SUCCESS) { delete row; return e; }
+
+    FftStep* col = nullptr;
+    if (d.rank == 2) {
+        col = new FftStep();
+        col->dbl = d.dbl; col->cols = true; col->sign = sign; col->n = ns;
+        col->ncols = row_ld_out; col->ld = row_ld_out;
+        col->plane = (i64)ns * row_ld_out;
+        col->nsig = planes * row_ld_out;
+        if (d.type == FFT_R2R) {
+            int kind = sign == FFT_FWD ? d.kind_slow : inverse_kind(d.kind_slow);
+            col->mode = mode_for_r2r(kind);
+            if (col->mode < 0) { delete row; delete col; return DTFFT_ERROR_INVALID_R2R_KINDS; }
+        } else {
+            col->mode = M_C2C;
+        }
+        e = prepare_step(*col, tables_);
+        if (e != DTFFT_SUCCESS) { delete row; delete col; return e; }
+    }
+    if (d.rank == 2 && d.type == FFT_R2C && sign == FFT_BWD) {
+        col->reads_out = false;
+        steps.push_back(col);   // in place on the (destroyable) complex input
+        steps.push_back(row);
+    } else {
+        steps.push_back(row);
+        if (col) { col->reads_out = true; steps.push_back(col); }
+    }
+    return DTFFT_SUCCESS;
+}
+
+dtfft_error_t FftPlan::execute(const void* in, void* out, int sign, cudaStream_t s) {
+    if (d_.batch == 0) return DTFFT_SUCCESS;
+    const std::vector<FftStep*>& steps = sign == FFT_FWD ? fwd_ : bwd_;
+    if (d_.rank == 1) return launch_step(*steps[0], in, out, s);
+    if (d_.type == FFT_R2C && sign == FFT_BWD) {
+        GB_TRY(launch_step(*steps[0], in, const_cast<void*>(in), s));
+        return launch_step(*steps[1], in, out, s);
+    }
+    GB_TRY(launch_step(*steps[0], in, out, s));
+    return launch_step(*steps[1], out, out, s);
+}
+
+// ---------------------------------------------------------------------------
+// FusedFT: batched C2C along the source's aligned axis + the box-list transpose
+// ---------------------------------------------------------------------------
+dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, FusedFT** out) {
+    *out = nullptr;
+    if (bl.copy || bl.host.empty()) return DTFFT_ERROR_INVALID_USAGE;
+    if (bl.elem != (dbl ? 16 : 8)) return DTFFT_ERROR_INVALID_USAGE;
+    // rows per CTA: 16 when the signal fits 32 threads, else as many as 512 threads allow
+    int E = 0, T = 0;
+    Schedule sch;
+    if (!make_reg_schedule(m, false, E, sch, T, 64) && !make_reg_schedule(m, false, E, sch, T, 256))
+        return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    int S = 1;   // rows per CTA: a power of two, at most 16 and (S*T) within the launch bound
+    while (S * 2 <= 16 && S * 2 * T <= (dbl ? 256 : 512)) S *= 2;
+    std::vector<FGroup> groups;
+    std::vector<FSeg> segs;
+    i64 ctas = 0;
+    size_t b = 0;
+    const std::vector<Box>& bx = bl.host;
+    while (b < bx.size()) {
+        const Box& f = bx[b];
+        FGroup g;
+        g.src_off = f.src_off - f.a0;
+        g.su = f.sb; g.sw = f.sc; g.nu = f.nb; g.nw = f.nc;
+        g.seg_first = (int)segs.size();
+        std::vector<FSeg> gs;
+        size_t e = b;
+        while (e < bx.size() && bx[e].src_off - bx[e].a0 == g.src_off && bx[e].nb == f.nb && bx[e].nc == f.nc &&
+               bx[e].sb == f.sb && bx[e].sc == f.sc) {
+            FSeg sgm;
+            sgm.i0 = bx[e].a0; sgm.i1 = bx[e].a0 + bx[e].na;
+            sgm.dst_off = bx[e].dst_off; sgm.di = bx[e].da_or_db; sgm.dw = bx[e].dc;
+            gs.push_back(sgm);
+            ++e;
+        }
+        std::sort(gs.begin(), gs.end(), [](const FSeg& x, const FSeg& y) { return x.i0 < y.i0; });
+        int cov = 0;
+        for (const FSeg& sgm : gs) { if (sgm.i0 != cov) return DTFFT_ERROR_INVALID_USAGE; cov = sgm.i1; }
+        if (cov != m) return DTFFT_ERROR_INVALID_USAGE;   // rows must hold the whole transform axis
+        for (const FSeg& sgm : gs)   // the write-out indexes a segment with 32-bit offsets
+            if ((i64)(sgm.i1 - sgm.i0) * sgm.di + 16 >= 0x7fffffffLL) return DTFFT_ERROR_INVALID_USAGE;
+        g.nseg = (int)gs.size();
+        segs.insert(segs.end(), gs.begin(), gs.end());
+        g.tiles_u = (g.nu + S - 1) / S;
+        g.cta_begin = ctas;
+        ctas += (i64)g.tiles_u * g.nw;
+        groups.push_back(g);
+        b = e;
+    }
+    if (ctas > 0x7fffffffLL) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    FusedFT* p = new FusedFT();
+    p->m_ = m; p->dbl_ = dbl; p->E_ = E; p->T_ = T; p->S_ = S; p->sched_ = sch;
+    p->ngroups_ = (int)groups.size();
+    p->ctas_ = ctas;
+    const size_t es = dbl ? 16 : 8;
+    const int pitch = m + m / 16;
+    p->pitch_ = pitch;
+    p->smem_ = std::max((size_t)S * pitch, (size_t)m * (S + 1)) * es;
+    // TMA-pipelined variant: every row start must be 16-byte aligned
+    bool aligned = (m * es) % 16 == 0;
+    for (const FGroup& g : groups)
+        aligned = aligned && (g.src_off * (i64)es) % 16 == 0 && (g.su * (i64)es) % 16 == 0 &&
+                  (g.sw * (i64)es) % 16 == 0;
+    if (aligned && !getenv("DTFFT_GB_NO_PIPE")) {
+        p->pipe_smem_ = 128 + 2 * (size_t)S * m * es + p->smem_;
+        p->pipe_per_sm_ = pipe_occupancy(dbl, m, E, true, S * T, p->pipe_smem_);
+    }
+    dtfft_error_t err = upload_table(table_exp(m, 1, m), dbl, p->owned_, &p->tw_);
+    if (err == DTFFT_SUCCESS) {
+        void* dg = nullptr; void* ds = nullptr;
+        if (cudaMalloc(&dg, sizeof(FGroup) * groups.size()) != cudaSuccess ||
+            cudaMalloc(&ds, sizeof(FSeg) * segs.size()) != cudaSuccess) {
+            err = DTFFT_ERROR_GPU_CALL_FAILED;
+        } else {
+            cudaMemcpy(dg, groups.data(), sizeof(FGroup) * groups.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(ds, segs.data(), sizeof(FSeg) * segs.size(), cudaMemcpyHostToDevice);
+        }
+        if (dg) p->owned_.push_back(dg);
+        if (ds) p->owned_.push_back(ds);
+        p->groups_ = dg; p->segs_ = ds;
+    }
+    if (err != DTFFT_SUCCESS) { delete p; return err; }
+    *out = p;
+    return DTFFT_SUCCESS;
+}
+
+FusedFT::~FusedFT() { for (void* t : owned_) cudaFree(t); }
+
+template <typename R>
+static dtfft_error_t launch_fused_t(const FusedFT& F, int m, int E, int T, int S, int pitch, const Schedule& sch,
+                                   const void* tw, const void* groups, const void* segs, int ngroups, i64 ctas,
+                                   size_t smem, const void* in, void* out, int sign, cudaStream_t s) {
+    typedef typename CT<R>::T C;
+    FArgs<R> A;
+    A.in = (const C*)in; A.out = (C*)out;
+    A.groups = (const FGroup*)groups; A.segs = (const FSeg*)segs; A.ngroups = ngroups;
+    A.m = m; A.sign = sign; A.S = S; A.pitch = pitch; A.tw = (const C*)tw;
+    A.st.ns = (int)sch.radix.size();
+    for (int i = 0; i < A.st.ns; ++i) A.st.radix[i] = sch.radix[i];
+    void (*kfn)(FArgs<R>) = (void (*)(FArgs<R>))KPtr<R>::xpose(E);
+    if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    if (smem > 48 * 1024)
+        GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared));
+    void* tok = prof_begin(s);
+    kfn<<<(unsigned)ctas, S * T, smem, s>>>(A);
+    if (tok) prof_end(tok, std::string("fftxpose_m") + std::to_string(m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
+    (void)F;
+    count_launch();
+    GB_CUDA_TRY(cudaGetLastError());
+    return DTFFT_SUCCESS;
+}
+
+template <typename R>
+static dtfft_error_t launch_fused_pipe(int m, int E, int T, int S, int pitch, const Schedule& sch, const void* tw,
+                                      const void* groups, const void* segs, int ngroups, i64 tiles, size_t smem,
+                                      int per_sm, const void* in, void* out, int sign, cudaStream_t s) {
+    typedef typename CT<R>::T C;
+    PArgs<R> P;
+    P.in = (const C*)in; P.out = (C*)out;
+    P.nsig = 0; P.groups = (const FGroup*)groups; P.segs = (const FSeg*)segs; P.ngroups = ngroups;
+    P.ntiles = tiles; P.m = m; P.sign = sign; P.S = S; P.pitch = pitch; P.nst = 2; P.tw = (const C*)tw;
+    P.st.ns = (int)sch.radix.size();
+    for (int i = 0; i < P.st.ns; ++i) P.st.radix[i] = sch.radix[i];
+    void* tok = prof_begin(s);
+    GB_TRY((launch_pipe<R, true>(P, E, S * T, smem, per_sm, s)));
+    if (tok) prof_end(tok, std::string("fftpipe_xpose_m") + std::to_string(m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
+    count_launch();
+    GB_CUDA_TRY(cudaGetLastError());
+    return DTFFT_SUCCESS;
+}
+
+dtfft_error_t FusedFT::execute(const void* in, void* out, int sign, cudaStream_t s) {
+    if (ctas_ == 0) return DTFFT_SUCCESS;
+    if (pipe_per_sm_ > 0 && ((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
+        if (dbl_)
+            return launch_fused_pipe<double>(m_, E_, T_, S_, pitch_, sched_, tw_, groups_, segs_, ngroups_, ctas_,
+                                             pipe_smem_, pipe_per_sm_, in, out, sign, s);
+        return launch_fused_pipe<float>(m_, E_, T_, S_, pitch_, sched_, tw_, groups_, segs_, ngroups_, ctas_,
+                                        pipe_smem_, pipe_per_sm_, in, out, sign, s);
+    }
+    if (dbl_)
+        return launch_fused_t<double>(*this, m_, E_, T_, S_, pitch_, sched_, tw_, groups_, segs_, ngroups_, ctas_,
+                                      smem_, in, out, sign, s);
+    return launch_fused_t<float>(*this, m_, E_, T_, S_, pitch_, sched_, tw_, groups_, segs_, ngroups_, ctas_, smem_,
+                                 in, out, sign, s);
+}
+
+}  // namespace gb
+
+extern "C" int32_t dtfft_gb_device_status(int32_t reset) {
+    int v = -1;
+    if (cudaMemcpyFromSymbol(&v, gb::g_gb_status, sizeof(int)) != cudaSuccess) { cudaGetLastError(); return -1; }
+    if (reset) {
+        int z = 0;
+        cudaMemcpyToSymbol(gb::g_gb_status, &z, sizeof(int));
+    }
+    return v;
+}

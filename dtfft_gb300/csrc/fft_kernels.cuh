@@ -1,3 +1,7 @@
+// Device code of the FFT kernels (templates only; instantiated per precision in
+// fft_inst_*.cu so the build compiles them in parallel).
+#pragma once
+
 // Stockham FFT kernels for the GB300 execute path.
 //
 // One CTA loads whole signals (contiguous rows, or TC adjacent columns of a
@@ -19,10 +23,8 @@
 //   DST-II/III/IV      : the matching DCT with (-1)^j signs and reversal
 // Conventions are FFTW's (unnormalised, sign -1 forward), which the reference
 // executors use (src/interfaces/fft/fftw/dtfft_executor_fftw_m.F90:91-226).
-#include <algorithm>
-#include <cmath>
-#include <cstdio>
-#include <sstream>
+
+#include <cstdint>
 
 #include "fft.cuh"
 
@@ -645,376 +647,410 @@ __global__ void __launch_bounds__(256) fft_reg_kernel(Args<R> A) {
     }
 }
 
-// ---------------------------------------------------------------------------
-// Host side
-// ---------------------------------------------------------------------------
-std::string Schedule::str() const {
-    std::ostringstream o;
-    for (size_t i = 0; i < radix.size(); ++i) o << (i ? "x" : "") << radix[i];
-    return o.str();
-}
-
-bool make_schedule(int m, Schedule& s) {
-    s.m = m;
-    s.radix.clear();
-    int r = m;
-    while (r % 8 == 0) { s.radix.push_back(8); r /= 8; }
-    if (r % 4 == 0) { s.radix.push_back(4); r /= 4; }
-    if (r % 2 == 0) { s.radix.push_back(2); r /= 2; }
-    const int small[] = {3, 5, 7};
-    for (int p : small) while (r % p == 0) { s.radix.push_back(p); r /= p; }
-    for (int p = 11; p <= 127 && r > 1; p += 2) {
-        bool prime = true;
-        for (int q = 3; q * q <= p; q += 2) if (p % q == 0) { prime = false; break; }
-        if (!prime) continue;
-        while (r % p == 0) { s.radix.push_back(p); r /= p; }
-    }
-    if (r != 1) return false;
-    if (s.radix.size() > 26) return false;
-    return true;
-}
-
-struct FftStep {
-    bool cols = false;
-    int dbl = 0;
-    int mode = M_C2C;
-    int sign = -1;
-    // geometry
-    i64 nsig = 0, idist = 0, odist = 0, plane = 0;
-    int ld = 0, ncols = 0, n = 0, m = 0, per = 1, pitch = 0;
-    const void* tw = nullptr;
-    const void* ta = nullptr;
-    const void* tb = nullptr;
-    Schedule sched;
-    size_t smem = 0;
-    int E = 0;               // points per thread of the register kernel, 0 = shared-memory kernel
-    int threads = 256;
-    bool reads_out = false;  // step reads the plan's output buffer (second pass)
+// ===========================================================================
+// Fused FFT + transpose (C2C)
+//
+// One pass replaces "FFT along the aligned axis" followed by "transpose to the
+// next pencil layout" of the reference's schedule (e.g. fft(1) then X->Y in
+// execute_generic, src/dtfft_plan.F90:1088-1090).  A CTA takes S rows of one
+// source rank block that are consecutive along the destination's contiguous
+// axis (u), transforms them in registers, stages the spectra in shared memory
+// as [point i][row] and writes, for every point i, the S values as one
+// contiguous run of the destination.  Point i belongs to the destination rank
+// whose segment [i0, i1) contains it; segments carry that rank's base offset
+// and strides, so the virtual-rank exchange costs nothing extra.
+// ===========================================================================
+struct FGroup {           // one source rank block
+    i64 src_off;          // element (i = 0, u = 0, w = 0) of the block
+    i64 su, sw;           // source strides of u and w (rows are contiguous)
+    int nu, nw;
+    int seg_first, nseg;
+    int tiles_u;
+    i64 cta_begin;
+};
+struct FSeg {             // points [i0, i1) of a group go to one destination rank
+    int i0, i1;
+    i64 dst_off;          // destination element of (i0, u = 0, w = 0); u has stride 1
+    i64 di, dw;
 };
 
-// Register-kernel schedule: points per thread E (compiled: 8, 16, 24, 20, 28),
-// radices dividing E, fewest stages first, then fewest registers.
-static bool make_reg_schedule(int m, bool cols, int& E_out, Schedule& sch, int& T_out) {
-    static const int Es[] = {8, 16, 24, 20, 28};
-    static const int rads[] = {16, 8, 7, 5, 4, 3, 2};
-    int best_stages = 1 << 30, best_E = 0;
-    Schedule best;
-    for (int E : Es) {
-        if (m % E != 0) continue;
-        const int T = m / E;
-        if (T < 1 || T > 256) continue;
-        if (cols && T > 64) continue;
-        Schedule s;
-        s.m = m;
-        int r = m;
-        while (r > 1) {
-            int pick = 0;
-            for (int q : rads)
-                if (E % q == 0 && r % q == 0) { pick = q; break; }
-            if (!pick) break;
-            s.radix.push_back(pick);
-            r /= pick;
-        }
-        if (r != 1) continue;
-        const int st = (int)s.radix.size();
-        if (st < best_stages || (st == best_stages && E < best_E)) { best_stages = st; best_E = E; best = s; }
-    }
-    if (!best_E) return false;
-    E_out = best_E;
-    T_out = m / best_E;
-    sch = best;
-    return true;
-}
-
-static int mode_for_r2r(int kind) {
-    switch (kind) {
-    case DTFFT_DCT_1: return M_DCT1;
-    case DTFFT_DCT_2: return M_DCT2;
-    case DTFFT_DCT_3: return M_DCT3;
-    case DTFFT_DCT_4: return M_DCT4;
-    case DTFFT_DST_1: return M_DST1;
-    case DTFFT_DST_2: return M_DST2;
-    case DTFFT_DST_3: return M_DST3;
-    case DTFFT_DST_4: return M_DST4;
-    }
-    return -1;
-}
-
-static int inverse_kind(int kind) {  // src/dtfft_utils.F90:447-471
-    switch (kind) {
-    case DTFFT_DCT_2: return DTFFT_DCT_3;
-    case DTFFT_DCT_3: return DTFFT_DCT_2;
-    case DTFFT_DST_2: return DTFFT_DST_3;
-    case DTFFT_DST_3: return DTFFT_DST_2;
-    default: return kind;
-    }
-}
-
-// Core length and core sign of a mode for a signal of logical length n.
-static bool mode_geometry(int mode, int n, int plan_sign, int& m, int& sign) {
-    sign = plan_sign;
-    switch (mode) {
-    case M_C2C: m = n; break;
-    case M_R2C_HALF: m = n / 2; sign = -1; break;
-    case M_R2C_FULL: m = n; sign = -1; break;
-    case M_C2R_HALF: m = n / 2; sign = 1; break;
-    case M_C2R_FULL: m = n; sign = 1; break;
-    case M_DCT1: if (n < 2) return false; m = 2 * (n - 1); sign = -1; break;
-    case M_DST1: m = 2 * (n + 1); sign = -1; break;
-    case M_DCT2: case M_DST2: m = n; sign = -1; break;
-    case M_DCT3: case M_DST3: m = n; sign = 1; break;
-    case M_DCT4: case M_DST4: m = 2 * n; sign = -1; break;
-    default: return false;
-    }
-    return m >= 1;
-}
-
-// Host table of exp(-2*pi*i*j*num/den) for j < count, built in double precision.
-static std::vector<double> table_exp(int count, long long num, long long den) {
-    std::vector<double> t(2 * (size_t)count);
-    for (int j = 0; j < count; ++j) {
-        // reduce j*num mod den exactly before converting to an angle
-        long long q = ((long long)j * num) % den;
-        double ang = -2.0 * M_PI * (double)q / (double)den;
-        t[2 * j] = std::cos(ang);
-        t[2 * j + 1] = std::sin(ang);
-    }
-    return t;
-}
-
-static dtfft_error_t upload_table(const std::vector<double>& t, int dbl, std::vector<void*>& owned, const void** out) {
-    size_t n = t.size();
-    void* d = nullptr;
-    if (dbl) {
-        GB_CUDA_TRY(cudaMalloc(&d, n * sizeof(double)));
-        GB_CUDA_TRY(cudaMemcpy(d, t.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-    } else {
-        std::vector<float> f(n);
-        for (size_t i = 0; i < n; ++i) f[i] = (float)t[i];
-        GB_CUDA_TRY(cudaMalloc(&d, n * sizeof(float)));
-        GB_CUDA_TRY(cudaMemcpy(d, f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
-    }
-    owned.push_back(d);
-    *out = d;
-    return DTFFT_SUCCESS;
-}
-
-static const size_t kSmemBudget = 96 * 1024;
-
-// Fill geometry, tables and launch shape of one step.
-static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
-    int m, sign;
-    if (!mode_geometry(S.mode, S.n, S.sign, m, sign)) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-    S.m = m;
-    S.sign = sign;
-    const size_t es = S.dbl ? 16 : 8;
-    int E = 0, T = 0;
-    if (!getenv("DTFFT_GB_NO_REG_FFT") && make_reg_schedule(m, S.cols, E, S.sched, T)) {
-        S.E = E;
-        // S signals per CTA, blockDim = S*T (signals past the end are masked)
-        S.per = std::max(1, 256 / T);
-        S.threads = S.per * T;
-        S.pitch = m + m / 16;
-        S.smem = S.cols ? (size_t)m * S.per * es : (size_t)S.per * S.pitch * es;
-    } else if (!make_schedule(m, S.sched)) {
-        return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-    }
-    if (S.E) goto tables;
-    {
-    const size_t per_sig = 2 * (size_t)m * es;   // ping-pong buffers
-    if (per_sig > 220 * 1024) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-    int per;
-    if (S.cols) {
-        per = S.dbl ? 8 : 16;
-        while (per > 1 && per * per_sig > 200 * 1024) per >>= 1;
-        per = std::min<i64>(per, S.ncols);
-        S.pitch = per;
-    } else {
-        per = (int)std::max<size_t>(1, kSmemBudget / per_sig);
-        // keep at least ~2 CTAs per SM worth of work when the batch is small
-        i64 want = std::max<i64>(1, S.nsig / (152 * 4));
-        per = (int)std::max<i64>(1, std::min<i64>(per, want));
-        per = std::min(per, 64);
-        S.pitch = m;
-    }
-    S.per = std::max(1, per);
-    S.smem = (size_t)S.per * per_sig;
-    }
-tables:
-    // tables
-    std::vector<double> tw = table_exp(m, 1, m);
-    GB_TRY(upload_table(tw, S.dbl, owned, &S.tw));
-    switch (S.mode) {
-    case M_R2C_HALF: GB_TRY(upload_table(table_exp(m + 1, 1, S.n), S.dbl, owned, &S.ta)); break;
-    case M_C2R_HALF: GB_TRY(upload_table(table_exp(m, 1, S.n), S.dbl, owned, &S.ta)); break;
-    case M_DCT2: case M_DST2: case M_DCT3: case M_DST3:
-        GB_TRY(upload_table(table_exp(S.n, 1, 4LL * S.n), S.dbl, owned, &S.ta)); break;
-    case M_DCT4: case M_DST4: {
-        GB_TRY(upload_table(table_exp(S.n, 1, 4LL * S.n), S.dbl, owned, &S.ta));
-        std::vector<double> t(2 * (size_t)S.n);
-        for (int k = 0; k < S.n; ++k) {
-            long long q = (2LL * k + 1) % (8LL * S.n);
-            double ang = -2.0 * M_PI * (double)q / (8.0 * S.n);
-            t[2 * k] = std::cos(ang); t[2 * k + 1] = std::sin(ang);
-        }
-        GB_TRY(upload_table(t, S.dbl, owned, &S.tb));
-    } break;
-    default: break;
-    }
-    return DTFFT_SUCCESS;
-}
-
-template <typename R, bool COLS>
-static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, cudaStream_t s) {
-    Args<R> A;
+template <typename R>
+struct FArgs {
     typedef typename CT<R>::T C;
-    A.in = (const char*)in; A.out = (char*)out;
-    A.nsig = S.nsig; A.idist = S.idist; A.odist = S.odist; A.plane = S.plane;
-    A.ld = S.ld; A.ncols = S.ncols; A.n = S.n; A.m = S.m; A.mode = S.mode; A.sign = S.sign;
-    A.per_cta = S.per; A.pitch = S.pitch;
-    A.tw = (const C*)S.tw; A.ta = (const C*)S.ta; A.tb = (const C*)S.tb;
-    A.st.ns = (int)S.sched.radix.size();
-    for (int i = 0; i < A.st.ns; ++i) A.st.radix[i] = S.sched.radix[i];
-    const i64 ctas = (S.nsig + S.per - 1) / S.per;
-    if (ctas <= 0) return DTFFT_SUCCESS;
-    if (ctas > 0x7fffffffLL) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-    void* tok = prof_begin(s);
-    if (S.E) {
-        void (*kfn)(Args<R>) = nullptr;
-        const bool c2c = S.mode == M_C2C;
-        switch (S.E) {
-        case 8: kfn = c2c ? fft_reg_kernel<R, 8, COLS, true> : fft_reg_kernel<R, 8, COLS, false>; break;
-        case 16: kfn = c2c ? fft_reg_kernel<R, 16, COLS, true> : fft_reg_kernel<R, 16, COLS, false>; break;
-        case 24: kfn = c2c ? fft_reg_kernel<R, 24, COLS, true> : fft_reg_kernel<R, 24, COLS, false>; break;
-        case 20: kfn = c2c ? fft_reg_kernel<R, 20, COLS, true> : fft_reg_kernel<R, 20, COLS, false>; break;
-        case 28: kfn = c2c ? fft_reg_kernel<R, 28, COLS, true> : fft_reg_kernel<R, 28, COLS, false>; break;
-        default: return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    const C* in;
+    C* out;
+    const FGroup* groups;
+    const FSeg* segs;
+    int ngroups;
+    int m, sign, S, pitch;
+    const C* tw;
+    Stages st;
+};
+
+template <typename R, int E>
+__global__ void __launch_bounds__(sizeof(R) == 8 ? 256 : 512) fft_xpose_kernel(FArgs<R> A) {
+    typedef typename CT<R>::T C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* sm = reinterpret_cast<C*>(smem_raw);
+    const int S = A.S, m = A.m, s = A.sign;
+    const int T = m / E;
+    const int sl = threadIdx.x / T, t = threadIdx.x % T;
+    // group of this CTA
+    const i64 cta = blockIdx.x;
+    int lo = 0, hi = A.ngroups - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.groups[mid].cta_begin <= cta) lo = mid; else hi = mid - 1;
+    }
+    const FGroup g = A.groups[lo];
+    const int tile = (int)(cta - g.cta_begin);
+    const int u0 = (tile % g.tiles_u) * S;
+    const int w = tile / g.tiles_u;
+    const int u = u0 + sl;
+    const bool live = u < g.nu;
+    const C* src = A.in + g.src_off + (i64)u * g.su + (i64)w * g.sw;
+
+    C v[E];
+#pragma unroll
+    for (int q = 0; q < E; ++q) {
+        if (live) v[q] = src[t + T * q];
+        else { v[q].x = 0; v[q].y = 0; }
+    }
+    int Ns = 1;
+    const int ns = A.st.ns;
+    for (int st = 0; st < ns - 1; ++st) {
+        const int rad = A.st.radix[st];
+        reg_stage_any<R, E, false, true>(rad, v, t, T, Ns, m, A.tw, s, sm, sl, A.pitch, S);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < E; ++q) v[q] = sm[rslot<false>(sl, t + T * q, A.pitch, S)];
+        __syncthreads();
+        Ns *= rad;
+    }
+    if (ns > 0) reg_stage_any<R, E, false, false>(A.st.radix[ns - 1], v, t, T, Ns, m, A.tw, s, sm, sl, A.pitch, S);
+    if (ns == 1) __syncthreads();   // no exchange ran: all loads precede the staging writes
+    // stage spectra as [i][row] (row stride S+1 keeps the column writes conflict-free)
+    const int SP = S + 1;
+#pragma unroll
+    for (int q = 0; q < E; ++q) sm[(t + T * q) * SP + sl] = v[q];
+    __syncthreads();
+    const int nu_here = min(S, g.nu - u0);
+    for (int k = 0; k < g.nseg; ++k) {
+        const FSeg sg = A.segs[g.seg_first + k];
+        const int cnt = (sg.i1 - sg.i0) * S;
+        C* dst = A.out + sg.dst_off + (i64)w * sg.dw + u0;
+        for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+            const int ii = e / S, r = e - ii * S;
+            if (r < nu_here) dst[(i64)ii * sg.di + r] = sm[(sg.i0 + ii) * SP + r];
         }
-        if (S.smem > 48 * 1024)
-            GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
-        kfn<<<(unsigned)ctas, S.threads, S.smem, s>>>(A);
+    }
+}
+
+// ===========================================================================
+// Pipelined persistent FFT kernels (TMA bulk copies + mbarriers)
+//
+// Persistent CTAs walk a list of tiles (S signals each).  One thread streams
+// the rows of upcoming tiles from HBM into a ring of NST shared-memory buffers
+// with cp.async.bulk (the Blackwell bulk-copy engine), completion tracked by a
+// transaction-count mbarrier per buffer.  The CTA transforms tile k while
+// tiles k+1 .. k+NST-1 are in flight, so HBM stays busy through the compute
+// and exchange phases.  Each thread reads its points t+T*q from the landed
+// buffer, runs the register stages, and stores straight to HBM (plain rows) or
+// through the [point][row] staging to each destination rank (fused transpose).
+//
+// Every mbarrier wait is bounded: on timeout the kernel records an error code
+// in g_gb_status, waits (bounded) for its own copies still in flight and
+// returns, leaving the context usable.
+// ===========================================================================
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst_smem, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst_smem)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok;
+}
+// bounded wait: false after ~2^22 polls (each poll may suspend the thread briefly)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+template <typename R>
+struct PArgs {
+    typedef typename CT<R>::T C;
+    const C* in;
+    C* out;
+    // plain rows: signal r at r*m, tile k = rows [k*S, k*S + S)
+    i64 nsig;
+    // fused: tiles are (group, u-tile, w)
+    const FGroup* groups;
+    const FSeg* segs;
+    int ngroups;
+    i64 ntiles;
+    int m, sign, S, pitch, nst;
+    const C* tw;
+    Stages st;
+    int* status;            // device status word (bounded-wait timeouts)
+};
+
+// Rows of tile `tile`: first source row, row stride, count (fused or plain).
+template <typename R, bool FUSED>
+__device__ __forceinline__ void tile_rows(const PArgs<R>& A, i64 tile, i64& row0, i64& rstride, int& nrows, int& gi,
+                                          int& u0, int& w) {
+    if (FUSED) {
+        int lo = 0, hi = A.ngroups - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (A.groups[mid].cta_begin <= tile) lo = mid; else hi = mid - 1;
+        }
+        const FGroup& g = A.groups[lo];
+        const int tl = (int)(tile - g.cta_begin);
+        u0 = (tl % g.tiles_u) * A.S;
+        w = tl / g.tiles_u;
+        nrows = min(A.S, g.nu - u0);
+        row0 = g.src_off + (i64)u0 * g.su + (i64)w * g.sw;
+        rstride = g.su;
+        gi = lo;
     } else {
-        if (S.smem > 48 * 1024)
-            GB_CUDA_TRY(cudaFuncSetAttribute(fft_kernel<R, COLS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
-        fft_kernel<R, COLS><<<(unsigned)ctas, 256, S.smem, s>>>(A);
+        row0 = tile * A.S * (i64)A.m;
+        nrows = (int)min((i64)A.S, A.nsig - tile * A.S);
+        rstride = A.m;
+        gi = 0; u0 = 0; w = 0;
     }
-    if (tok) {
-        static const char* mn[] = {"c2c", "r2c", "r2c", "c2r", "c2r", "dct1", "dct2", "dct3", "dct4",
-                                   "dst1", "dst2", "dst3", "dst4"};
-        prof_end(tok, std::string(S.E ? "fftreg_" : "fft_") + (COLS ? "cols_" : "rows_") + mn[S.mode] + "_m" +
-                          std::to_string(S.m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
+}
+
+template <typename R, bool FUSED>
+__device__ __forceinline__ void issue_tile(const PArgs<R>& A, i64 tile, typename CT<R>::T* buf, uint64_t* bar) {
+    typedef typename CT<R>::T C;
+    i64 row0, rs;
+    int nrows, gi, u0, w;
+    tile_rows<R, FUSED>(A, tile, row0, rs, nrows, gi, u0, w);
+    const uint32_t row_bytes = (uint32_t)(A.m * sizeof(C));
+    mbar_expect_tx(bar, row_bytes * (uint32_t)nrows);
+    if (rs == A.m) {
+        bulk_load(buf, A.in + row0, row_bytes * (uint32_t)nrows, bar);
+    } else {
+        for (int r = 0; r < nrows; ++r) bulk_load(buf + (i64)r * A.m, A.in + row0 + (i64)r * rs, row_bytes, bar);
     }
-    count_launch();
-    GB_CUDA_TRY(cudaGetLastError());
-    return DTFFT_SUCCESS;
 }
 
-static dtfft_error_t launch_step(const FftStep& S, const void* in, void* out, cudaStream_t s) {
-    if (S.dbl) return S.cols ? launch_step_t<double, true>(S, in, out, s) : launch_step_t<double, false>(S, in, out, s);
-    return S.cols ? launch_step_t<float, true>(S, in, out, s) : launch_step_t<float, false>(S, in, out, s);
-}
+// ---- stage schedules: runtime (any supported length) or compile time (hot lengths) ----
+template <int E_>
+struct RtSch {
+    static constexpr int E = E_;
+    static constexpr bool CT = false;
+};
+template <int E_, int... Rs>
+struct CtSch {
+    static constexpr int E = E_;
+    static constexpr bool CT = true;
+    static constexpr int M = (Rs * ... * 1);
+    static constexpr int T = M / E_;
+};
 
-dtfft_error_t FftPlan::create(const FftDesc& d, FftPlan** out) {
-    *out = nullptr;
-    if (d.rank != 1 && d.rank != 2) return DTFFT_ERROR_INVALID_USAGE;
-    if (d.n_fast < 1 || d.n_slow < 1 || d.batch < 0) return DTFFT_ERROR_INVALID_DIMENSION_SIZE;
-    FftPlan* p = new FftPlan();
-    p->d_ = d;
-    dtfft_error_t e = p->build(FFT_FWD, p->fwd_);
-    if (e == DTFFT_SUCCESS) e = p->build(FFT_BWD, p->bwd_);
-    if (e != DTFFT_SUCCESS) { delete p; return e; }
-    p->launches_ = (int)p->fwd_.size();
-    *out = p;
-    return DTFFT_SUCCESS;
-}
-
-FftPlan::~FftPlan() {
-    for (auto* s : fwd_) delete s;
-    for (auto* s : bwd_) delete s;
-    for (void* t : tables_) cudaFree(t);
-}
-
-// Steps of one direction:
-//   rank 1: one row step (any mode)
-//   rank 2: row step along n_fast, then an in-place column step along n_slow
-//           (C2R runs the column step first, on the input, then the row step)
-dtfft_error_t FftPlan::build(int sign, std::vector<FftStep*>& steps) {
-    const FftDesc& d = d_;
-    const int nf = d.n_fast, ns = d.n_slow;
-    const i64 planes = d.batch;
-    // row step
-    FftStep* row = new FftStep();
-    row->dbl = d.dbl; row->cols = false; row->sign = sign; row->n = nf;
-    row->nsig = planes * (d.rank == 2 ? ns : 1);
-    int row_ld_out = nf;  // complex row length after the row step (for the column step)
-    i64 in_row = d.rank == 2 ? 0 : d.idist, out_row = d.rank == 2 ? 0 : d.odist;
-    switch (d.type) {
-    case FFT_C2C:
-        row->mode = M_C2C;
-        if (d.rank == 2) { in_row = nf; out_row = nf; }
-        break;
-    case FFT_R2C:
-        if (sign == FFT_FWD) row->mode = (nf % 2 == 0) ? M_R2C_HALF : M_R2C_FULL;
-        else row->mode = (nf % 2 == 0) ? M_C2R_HALF : M_C2R_FULL;
-        row_ld_out = nf / 2 + 1;
-        if (d.rank == 2) {
-            if (sign == FFT_FWD) { in_row = nf; out_row = nf / 2 + 1; }
-            else { in_row = nf / 2 + 1; out_row = nf; }
+// One compile-time radix stage: T, M, RAD and Ns are constants, so the
+// butterfly index, the twiddle exponent and the exchange address reduce to
+// per-thread bases plus immediate offsets.
+template <typename R, int E, int T, int M, int RAD, int Ns, bool EX>
+__device__ __forceinline__ void ct_stage(typename CT<R>::T (&v)[E], int t, const typename CT<R>::T* __restrict__ tw,
+                                         int s, typename CT<R>::T* xrow) {
+    typedef typename CT<R>::T C;
+    constexpr int B = E / RAD;
+    constexpr int tstep = M / (Ns * RAD);
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = t + b * T;
+        const int k = (T % Ns == 0) ? (t % Ns) : (j % Ns);
+        C w[RAD];
+#pragma unroll
+        for (int r = 0; r < RAD; ++r) w[r] = v[b + r * B];
+        if constexpr (Ns > 1) {
+            const int e1 = tstep * k;   // W^0 = 1 sits at tw[0]: no branch on k
+#pragma unroll
+            for (int r = 1; r < RAD; ++r) {
+                C tv = __ldg(&tw[e1 * r]);
+                if (s > 0) tv.y = -tv.y;
+                w[r] = cmul(w[r], tv);
+            }
         }
-        break;
-    case FFT_R2R: {
-        int kind = sign == FFT_FWD ? d.kind_fast : inverse_kind(d.kind_fast);
-        row->mode = mode_for_r2r(kind);
-        if (row->mode < 0) { delete row; return DTFFT_ERROR_INVALID_R2R_KINDS; }
-        if (d.rank == 2) { in_row = nf; out_row = nf; }
-    } break;
-    default: delete row; return DTFFT_ERROR_INVALID_USAGE;
-    }
-    // rank 1: idist/odist describe the forward (real -> complex) direction;
-    // the C2R step reads complex rows odist apart and writes real rows idist apart
-    if (d.rank == 1 && d.type == FFT_R2C && sign == FFT_BWD) std::swap(in_row, out_row);
-    row->idist = in_row; row->odist = out_row;
-    dtfft_error_t e = prepare_step(*row, tables_);
-    if (e != DTFFT_SUCCESS) { delete row; return e; }
-
-    FftStep* col = nullptr;
-    if (d.rank == 2) {
-        col = new FftStep();
-        col->dbl = d.dbl; col->cols = true; col->sign = sign; col->n = ns;
-        col->ncols = row_ld_out; col->ld = row_ld_out;
-        col->plane = (i64)ns * row_ld_out;
-        col->nsig = planes * row_ld_out;
-        if (d.type == FFT_R2R) {
-            int kind = sign == FFT_FWD ? d.kind_slow : inverse_kind(d.kind_slow);
-            col->mode = mode_for_r2r(kind);
-            if (col->mode < 0) { delete row; delete col; return DTFFT_ERROR_INVALID_R2R_KINDS; }
+        dft_any<R, RAD>(w, s);
+        if constexpr (EX) {
+            const int base = (j - k) * RAD + k;
+#pragma unroll
+            for (int r = 0; r < RAD; ++r) xrow[rpad(base + r * Ns)] = w[r];
         } else {
-            col->mode = M_C2C;
+#pragma unroll
+            for (int r = 0; r < RAD; ++r) v[b + r * B] = w[r];
         }
-        e = prepare_step(*col, tables_);
-        if (e != DTFFT_SUCCESS) { delete row; delete col; return e; }
     }
-    if (d.rank == 2 && d.type == FFT_R2C && sign == FFT_BWD) {
-        col->reads_out = false;
-        steps.push_back(col);   // in place on the (destroyable) complex input
-        steps.push_back(row);
-    } else {
-        steps.push_back(row);
-        if (col) { col->reads_out = true; steps.push_back(col); }
-    }
-    return DTFFT_SUCCESS;
 }
 
-dtfft_error_t FftPlan::execute(const void* in, void* out, int sign, cudaStream_t s) {
-    if (d_.batch == 0) return DTFFT_SUCCESS;
-    const std::vector<FftStep*>& steps = sign == FFT_FWD ? fwd_ : bwd_;
-    if (d_.rank == 1) return launch_step(*steps[0], in, out, s);
-    if (d_.type == FFT_R2C && sign == FFT_BWD) {
-        GB_TRY(launch_step(*steps[0], in, const_cast<void*>(in), s));
-        return launch_step(*steps[1], in, out, s);
+template <typename R, int E, int T, int M, int Ns, int RAD, int... Rest>
+__device__ __forceinline__ void ct_stages(typename CT<R>::T (&v)[E], int t, const typename CT<R>::T* tw, int s,
+                                          typename CT<R>::T* xrow) {
+    if constexpr (sizeof...(Rest) == 0) {
+        ct_stage<R, E, T, M, RAD, Ns, false>(v, t, tw, s, xrow);
+    } else {
+        ct_stage<R, E, T, M, RAD, Ns, true>(v, t, tw, s, xrow);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < E; ++q) v[q] = xrow[rpad(t + T * q)];
+        __syncthreads();
+        ct_stages<R, E, T, M, Ns * RAD, Rest...>(v, t, tw, s, xrow);
     }
-    GB_TRY(launch_step(*steps[0], in, out, s));
-    return launch_step(*steps[1], out, out, s);
 }
+
+template <typename R, int E, int... Rs>
+__device__ __forceinline__ void run_sched(CtSch<E, Rs...>, typename CT<R>::T (&v)[E], int t, int T, int m,
+                                          const Stages&, const typename CT<R>::T* tw, int s, typename CT<R>::T* xbuf,
+                                          int sl, int pitch, int S) {
+    (void)T; (void)m; (void)S;
+    ct_stages<R, E, CtSch<E, Rs...>::T, CtSch<E, Rs...>::M, 1, Rs...>(v, t, tw, s, xbuf + (i64)sl * pitch);
+}
+
+template <typename R, int E>
+__device__ __forceinline__ void run_sched(RtSch<E>, typename CT<R>::T (&v)[E], int t, int T, int m, const Stages& st_,
+                                          const typename CT<R>::T* tw, int s, typename CT<R>::T* xbuf, int sl, int pitch,
+                                          int S) {
+    int Ns = 1;
+    const int ns = st_.ns;
+    for (int st = 0; st < ns - 1; ++st) {
+        const int rad = st_.radix[st];
+        reg_stage_any<R, E, false, true>(rad, v, t, T, Ns, m, tw, s, xbuf, sl, pitch, S);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < E; ++q) v[q] = xbuf[rslot<false>(sl, t + T * q, pitch, S)];
+        __syncthreads();
+        Ns *= rad;
+    }
+    if (ns > 0) reg_stage_any<R, E, false, false>(st_.radix[ns - 1], v, t, T, Ns, m, tw, s, xbuf, sl, pitch, S);
+}
+
+template <typename R, typename SCH, bool FUSED>
+__global__ void __launch_bounds__(sizeof(R) == 8 ? 256 : 512) fft_pipe_kernel(PArgs<R> A) {
+    typedef typename CT<R>::T C;
+    constexpr int E = SCH::E;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+    const int S = A.S, m = A.m, s = A.sign, NST = A.nst;
+    C* inbuf = reinterpret_cast<C*>(smem_raw + 128);
+    C* xbuf = inbuf + (i64)NST * S * m;
+    const int T = m / E;
+    const int sl = threadIdx.x / T, t = threadIdx.x % T;
+
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < NST; ++b) mbar_init(&bars[b], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int j = 0; j < NST; ++j) {
+            const i64 tj = blockIdx.x + (i64)j * gridDim.x;
+            if (tj < A.ntiles) issue_tile<R, FUSED>(A, tj, inbuf + (i64)j * S * m, &bars[j]);
+        }
+    }
+    int k = 0;
+    for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x, ++k) {
+        const int b = k % NST;
+        const uint32_t par = (uint32_t)((k / NST) & 1);
+        const bool ok = mbar_wait_bounded(&bars[b], par);
+        if (__syncthreads_or(!ok)) {
+            // give up: record, drain this CTA's copies still in flight, leave
+            if (threadIdx.x == 0) {
+                atomicExch(A.status, 1);
+                for (int j = 0; j < NST; ++j) {
+                    const i64 tj = tile + (i64)j * gridDim.x;
+                    if (tj >= A.ntiles) break;
+                    mbar_wait_bounded(&bars[(k + j) % NST], (uint32_t)(((k + j) / NST) & 1));
+                }
+            }
+            __syncthreads();
+            return;
+        }
+        i64 row0, rs;
+        int nrows, gi, u0, w;
+        tile_rows<R, FUSED>(A, tile, row0, rs, nrows, gi, u0, w);
+        const bool live = sl < nrows;
+        const C* mine = inbuf + (i64)b * S * m + (i64)sl * m;
+        C v[E];
+#pragma unroll
+        for (int q = 0; q < E; ++q) v[q] = mine[t + T * q];
+        __syncthreads();   // buffer b fully read: refill it with tile + NST*grid
+        if (threadIdx.x == 0) {
+            fence_async_smem();
+            const i64 tn = tile + (i64)NST * gridDim.x;
+            if (tn < A.ntiles) issue_tile<R, FUSED>(A, tn, inbuf + (i64)b * S * m, &bars[b]);
+        }
+        run_sched<R>(SCH{}, v, t, T, m, A.st, A.tw, s, xbuf, sl, A.pitch, S);
+        if constexpr (!FUSED) {
+            if (live) {
+                C* dst = A.out + row0 + (i64)sl * m;
+#pragma unroll
+                for (int q = 0; q < E; ++q) dst[t + T * q] = v[q];
+            }
+        } else {
+            const int SP = S + 1;
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < E; ++q) xbuf[(t + T * q) * SP + sl] = v[q];
+            __syncthreads();
+            const FGroup& g = A.groups[gi];
+            const int lgS = __ffs(S) - 1;   // S is a power of two
+            for (int kk = 0; kk < g.nseg; ++kk) {
+                const FSeg sg = A.segs[g.seg_first + kk];
+                const int cnt = (sg.i1 - sg.i0) << lgS;
+                C* dst = A.out + sg.dst_off + (i64)w * sg.dw + u0;
+                const int di = (int)sg.di;
+                const C* src = xbuf + sg.i0 * SP;
+                for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+                    const int ii = e >> lgS, r = e & (S - 1);
+                    if (r < nrows) dst[ii * di + r] = src[ii * SP + r];
+                }
+            }
+        }
+    }
+}
+
+
+// Lengths with a compile-time schedule, and their points per thread.
+inline int ct_points_per_thread(int m) {
+    switch (m) {
+    case 8: case 32: case 64: case 512: return 8;
+    case 16: case 128: case 256: case 1024: case 2048: case 4096: return 16;
+    case 96: case 384: case 768: return 24;
+    }
+    return 0;
+}
+
+// Kernel entry points of one precision (defined in fft_inst_f32.cu / fft_inst_f64.cu).
+template <typename R>
+struct KPtr {
+    static void* reg(int E, bool cols, bool c2c);    // fft_reg_kernel
+    static void* generic(bool cols);                 // fft_kernel
+    static void* xpose(int E);                       // fft_xpose_kernel
+    static void* pipe(int m, int E, bool fused);     // fft_pipe_kernel
+};
 
 }  // namespace gb

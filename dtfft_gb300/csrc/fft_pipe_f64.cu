@@ -1,0 +1,40 @@
+// Pipelined-kernel instantiations for double precision.
+#include "fft_kernels.cuh"
+
+namespace gb {
+
+template <bool F>
+static void* pipe_ptr(int m, int E) {
+    if (E == ct_points_per_thread(m)) {
+        switch (m) {
+        case 8: return (void*)fft_pipe_kernel<double, CtSch<8, 8>, F>;
+        case 16: return (void*)fft_pipe_kernel<double, CtSch<16, 16>, F>;
+        case 32: return (void*)fft_pipe_kernel<double, CtSch<8, 8, 4>, F>;
+        case 64: return (void*)fft_pipe_kernel<double, CtSch<8, 8, 8>, F>;
+        case 128: return (void*)fft_pipe_kernel<double, CtSch<16, 16, 8>, F>;
+        case 256: return (void*)fft_pipe_kernel<double, CtSch<16, 16, 16>, F>;
+        case 512: return (void*)fft_pipe_kernel<double, CtSch<8, 8, 8, 8>, F>;
+        case 1024: return (void*)fft_pipe_kernel<double, CtSch<16, 16, 8, 8>, F>;
+        case 2048: return (void*)fft_pipe_kernel<double, CtSch<16, 16, 16, 8>, F>;
+        case 4096: return (void*)fft_pipe_kernel<double, CtSch<16, 16, 16, 16>, F>;
+        case 96: return (void*)fft_pipe_kernel<double, CtSch<24, 8, 4, 3>, F>;
+        case 384: return (void*)fft_pipe_kernel<double, CtSch<24, 8, 8, 2, 3>, F>;
+        case 768: return (void*)fft_pipe_kernel<double, CtSch<24, 8, 8, 4, 3>, F>;
+        }
+    }
+    switch (E) {
+    case 8: return (void*)fft_pipe_kernel<double, RtSch<8>, F>;
+    case 16: return (void*)fft_pipe_kernel<double, RtSch<16>, F>;
+    case 24: return (void*)fft_pipe_kernel<double, RtSch<24>, F>;
+    case 20: return (void*)fft_pipe_kernel<double, RtSch<20>, F>;
+    case 28: return (void*)fft_pipe_kernel<double, RtSch<28>, F>;
+    }
+    return nullptr;
+}
+
+template <>
+void* KPtr<double>::pipe(int m, int E, bool fused) {
+    return fused ? pipe_ptr<true>(m, E) : pipe_ptr<false>(m, E);
+}
+
+}  // namespace gb

@@ -223,6 +223,7 @@ BoxList make_boxes(const Layout& S, const Layout& R, int elem) {
             b.dst_off = R.off[j];
             for (int d = 0; d < nd; ++d) b.dst_off += (i64)(lo[R.axes[d]] - rj.start[d]) * rstr[d];
             b.na = hi[a_ax] - lo[a_ax];
+            b.a0 = lo[a_ax] - si.start[0];
             if (bl.copy) {
                 b.nb = hi[b2_ax] - lo[b2_ax];
                 b.sb = sstr[pos(S, b2_ax)];

@@ -36,6 +36,7 @@ struct Plan {
     int real_elem = 4;          // bytes of a real element
     BoxList tr[7];              // index transpose_type + 3
     FftPlan* fft[3] = {nullptr, nullptr, nullptr};
+    FusedFT* ft[7] = {};        // FFT on the send layout fused with transpose t (index t + 3)
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     void* aux = nullptr;
@@ -46,6 +47,7 @@ struct Plan {
     ~Plan() {
         for (auto& b : tr) boxes_free(b);
         for (auto*& f : fft) { delete f; f = nullptr; }
+        for (auto*& f : ft) { delete f; f = nullptr; }
         if (aux) cudaFree(aux);
         if (own_stream && stream) cudaStreamDestroy(stream);
         magic = 0;
@@ -180,6 +182,27 @@ static dtfft_error_t build_ffts(Plan& p) {
     return DTFFT_SUCCESS;
 }
 
+// Fused FFT + transpose steps of the generic and 2D schedules (C2C axes only).
+// A step that does not fit the fused kernel keeps the two-kernel form.
+static void build_fused(Plan& p) {
+    if (p.transpose_only || p.kind == K_R2R || p.z_slab || p.y_slab) return;
+    // opt-in until the fused pass beats FFT + transpose on the target sizes
+    const char* fz = getenv("DTFFT_GB_FUSE");
+    if (!fz || strcmp(fz, "0") == 0) return;
+    const int dbl = p.precision == DTFFT_DOUBLE ? 1 : 0;
+    std::vector<std::pair<int, int>> steps;   // (transpose type, FFT dim on its send layout)
+    if (p.ndims == 2) steps = {{1, 1}, {-1, 2}};
+    else steps = {{1, 1}, {2, 2}, {-2, 3}, {-1, 2}};
+    for (auto st : steps) {
+        const int t = st.first, d = st.second;
+        if (p.kind == K_R2C && d == 1) continue;   // the X axis is R2C
+        const BoxList& bl = p.tr[t + 3];
+        if (bl.host.empty() || !p.fft[d - 1]) continue;
+        FusedFT* f = nullptr;
+        if (FusedFT::create(bl, p.pen[d - 1].gsize[0], dbl, &f) == DTFFT_SUCCESS) p.ft[t + 3] = f;
+    }
+}
+
 static dtfft_error_t create_plan(int kind, int8_t ndims, const int32_t* dims, const int32_t* kinds,
                                  MPI_Comm comm, dtfft_precision_t precision, dtfft_effort_t effort,
                                  dtfft_executor_t executor, dtfft_plan_t* out) {
@@ -231,6 +254,7 @@ static dtfft_error_t create_plan(int kind, int8_t ndims, const int32_t* dims, co
     }
     if (e == DTFFT_SUCCESS) e = build_transposes(*p);
     if (e == DTFFT_SUCCESS) e = build_ffts(*p);
+    if (e == DTFFT_SUCCESS) build_fused(*p);
     if (e == DTFFT_SUCCESS && (effort == DTFFT_EXHAUSTIVE || cfg.enable_kernel_autotune)) {
         for (auto& bl : p->tr) {
             if (bl.host.empty()) continue;
@@ -287,12 +311,12 @@ static dtfft_error_t run_execute(Plan& p, void* in, void* out, bool fwd, void* a
     if (p.ndims == 2 || p.y_slab) {
         if (p.transpose_only) return T(p, fwd ? 1 : -1, in, out);
         if (fwd) {
-            GB_TRY(F(p, 1, in, aux, S));
-            GB_TRY(T(p, 1, aux, out));
+            if (p.ft[1 + 3]) GB_TRY(p.ft[1 + 3]->execute(in, out, S, p.stream));   // fft(1) + X->Y
+            else { GB_TRY(F(p, 1, in, aux, S)); GB_TRY(T(p, 1, aux, out)); }
             return F(p, 2, out, out, S);
         }
-        GB_TRY(F(p, 2, in, in, S));
-        GB_TRY(T(p, -1, in, aux));
+        if (p.ft[-1 + 3]) GB_TRY(p.ft[-1 + 3]->execute(in, aux, S, p.stream));      // fft(2) + Y->X
+        else { GB_TRY(F(p, 2, in, in, S)); GB_TRY(T(p, -1, in, aux)); }
         return F(p, 1, aux, out, S);
     }
     if (p.z_slab && !(p.transpose_only && inplace)) {
@@ -311,18 +335,22 @@ static dtfft_error_t run_execute(Plan& p, void* in, void* out, bool fwd, void* a
         GB_TRY(T(p, -2, in, aux));
         return T(p, -1, aux, out);
     }
+    // generic schedule; an FFT and the transpose after it run as one fused pass
+    // when the plan built one (the buffer roles of the reference are kept)
     if (fwd) {
-        GB_TRY(F(p, 1, in, aux, S));
-        GB_TRY(T(p, 1, aux, out));
-        GB_TRY(F(p, 2, out, out, S));
-        GB_TRY(T(p, 2, out, aux));
+        if (p.ft[1 + 3]) GB_TRY(p.ft[1 + 3]->execute(in, out, S, p.stream));       // fft(1) + X->Y
+        else { GB_TRY(F(p, 1, in, aux, S)); GB_TRY(T(p, 1, aux, out)); }
+        if (p.ft[2 + 3]) GB_TRY(p.ft[2 + 3]->execute(out, aux, S, p.stream));      // fft(2) + Y->Z
+        else { GB_TRY(F(p, 2, out, out, S)); GB_TRY(T(p, 2, out, aux)); }
         return F(p, 3, aux, out, S);
     }
-    GB_TRY(F(p, 3, in, aux, S));
-    GB_TRY(T(p, -2, aux, in));
-    GB_TRY(F(p, 2, in, in, S));
-    GB_TRY(T(p, -1, in, aux));
-    return F(p, 1, aux, out, S);
+    void* cur;
+    if (p.ft[-2 + 3]) { GB_TRY(p.ft[-2 + 3]->execute(in, aux, S, p.stream)); cur = aux; }   // fft(3) + Z->Y
+    else { GB_TRY(F(p, 3, in, aux, S)); GB_TRY(T(p, -2, aux, in)); cur = in; }
+    void* other = cur == aux ? in : aux;
+    if (p.ft[-1 + 3]) GB_TRY(p.ft[-1 + 3]->execute(cur, other, S, p.stream));             // fft(2) + Y->X
+    else { GB_TRY(F(p, 2, cur, cur, S)); GB_TRY(T(p, -1, cur, other)); }
+    return F(p, 1, other, out, S);
 }
 
 struct Request { uint32_t magic; int type; };

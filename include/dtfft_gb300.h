@@ -134,6 +134,14 @@ dtfft_error_t dtfft_vgrid_get_pencil(dtfft_plan_t plan, dtfft_layout_t layout, i
 /** Number of launches of this library's kernels since load (for benchmarks). */
 int64_t dtfft_gb_kernel_launch_count(void);
 
+/**
+ * Device-side status word of the pipelined kernels: 0 = fine, 1 = a bounded
+ * wait on a bulk-copy barrier gave up (the kernel drained its copies and
+ * returned; results of that launch are incomplete).  Synchronises the device;
+ * `reset` != 0 clears the word afterwards.  -1 if it could not be read.
+ */
+int32_t dtfft_gb_device_status(int32_t reset);
+
 /* ------------------------------------------------------------------------ */
 /* Kernel timing (for benchmarks)                                            */
 /* Between start and stop every launch is bracketed by CUDA events on its    */

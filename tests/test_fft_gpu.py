@@ -60,6 +60,42 @@ def test_c2c_forward_backward(dt, orc, cuda, dims, grid, np_dtype):
     plan.destroy()
 
 
+@pytest.mark.parametrize("dims,grid,np_dtype", [
+    ([64, 48, 40], [1, 2, 4], np.complex64),
+    ([512, 32, 24], [1, 2, 2], np.complex64),
+    ([48, 36, 40], [1, 3, 2], np.complex128),
+    ([96, 64], [1, 2], np.complex64),
+    ([32, 24, 40], [1, 1, 1], np.float32),          # R2C: Y and Z axes fuse
+])
+def test_fused_fft_transpose(dt, orc, cuda, monkeypatch, dims, grid, np_dtype):
+    """Plans built with the fused FFT + transpose passes (DTFFT_GB_FUSE=1)."""
+    monkeypatch.setenv("DTFFT_GB_FUSE", "1")
+    nd = len(dims)
+    cfg = dt.Config(enable_z_slab=False)
+    if np_dtype == np.float32:
+        plan = dt.PlanR2C(dims, comm=comm_for(dt, grid), precision=dt.Precision.SINGLE,
+                          executor=dt.Executor.CUFFT, config=cfg)
+        cdt = np.complex64
+    else:
+        plan = dt.PlanC2C(dims, comm=comm_for(dt, grid), precision=_prec(dt, np_dtype),
+                          executor=dt.Executor.CUFFT, config=cfg)
+        cdt = np_dtype
+    dt.set_config(dt.Config())
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=11)
+    x = orc.global_to_packed(g, nd, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, cdt, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    kind = "r2c" if np_dtype == np.float32 else "c2c"
+    expect = orc.global_to_packed(orc.forward_values(g, kind), nd, grid, _final_layout(plan, nd))
+    assert orc.rel_l2(from_dev(b, expect.size, cdt), expect) <= TOL[np_dtype]
+    c = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    back = from_dev(c, x.size, np_dtype) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= TOL[np_dtype]
+    plan.destroy()
+
+
 def test_c2c_schedules_agree(dt, orc, cuda):
     """Z-slab, Y-slab and the generic 3-pencil schedule give the same spectrum."""
     dims = [64, 64, 64]
@@ -223,3 +259,11 @@ def test_fft_plugin_r2c(dt, cuda, n):
     torch.cuda.synchronize()
     assert np.linalg.norm(c.cpu().numpy() / n - x) / np.linalg.norm(x) <= 1e-12
     L.gb_fft_destroy(ctypes.byref(h))
+
+
+def test_device_status_clean_after_runs(dt, cuda):
+    """No bounded wait of the pipelined kernels gave up during the GPU tests."""
+    import torch
+    torch.cuda.synchronize()
+    dt.lib().dtfft_gb_device_status.restype = ctypes.c_int32
+    assert dt.lib().dtfft_gb_device_status(0) == 0
