@@ -451,6 +451,31 @@ dtfft_error_t dtfft_execute(dtfft_plan_t plan, void* in, void* out, dtfft_execut
     return run_execute(*p, in, out, execute_type == DTFFT_EXECUTE_FORWARD, a, inplace);
 }
 
+}  // extern "C"
+
+namespace gb {
+// Execute with caller-provided scratch of `scratch_bytes` (used by the
+// no-allocation entry point in noalloc.cu): the checks of dtfft_execute, then
+// the same schedule with `scratch` as aux.  Never allocates.
+dtfft_error_t execute_into_scratch(dtfft_plan_t plan, void* in, void* out, int execute_type, void* scratch,
+                                   size_t scratch_bytes, size_t* needed) {
+    if (!in || !out) return DTFFT_ERROR_INVALID_USAGE;
+    Plan* p = as_plan(plan);
+    if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
+    if (execute_type != DTFFT_EXECUTE_FORWARD && execute_type != DTFFT_EXECUTE_BACKWARD)
+        return DTFFT_ERROR_INVALID_EXECUTE_TYPE;
+    const bool inplace = in == out;
+    if (p->transpose_only && inplace && (p->ndims == 2 || p->y_slab)) return DTFFT_ERROR_INPLACE_TRANSPOSE;
+    if (p->transpose_only && p->kind == K_R2C) return DTFFT_ERROR_R2C_EXECUTE_CALLED;
+    if (needed) *needed = p->alloc_bytes();
+    if (p->alloc_bytes() > scratch_bytes) return DTFFT_ERROR_NOALLOC_SCRATCH_TOO_SMALL;
+    GB_TRY(check_ptrs(in, out, nullptr));
+    return run_execute(*p, in, out, execute_type == DTFFT_EXECUTE_FORWARD, scratch, inplace);
+}
+}  // namespace gb
+
+extern "C" {
+
 static dtfft_error_t transpose_checks(Plan* p, void* in, void* out, int t, void* aux) {
     const bool valid = (t >= -3 && t <= 3 && t != 0);
     if (!valid || (p->ndims == 2 && std::abs(t) > 1) || (std::abs(t) == 3 && !p->z_slab))

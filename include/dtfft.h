@@ -117,7 +117,10 @@ typedef enum {
     /* Library-specific: a CUDA call failed; the plan stays usable. */
     DTFFT_ERROR_GPU_CALL_FAILED = 600,
     /* Library-specific: a transform size this build's FFT kernels cannot run. */
-    DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED = 601
+    DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED = 601,
+    /* Library-specific: the plan needs more scratch than the fixed buffer of
+     * dtfft_execute_noalloc holds (dtfft_gb300.h). */
+    DTFFT_ERROR_NOALLOC_SCRATCH_TOO_SMALL = 602
 } dtfft_error_t;
 
 /** Prints the failing call and aborts (reference: include/dtfft.h:62-70, which calls MPI_Abort). */

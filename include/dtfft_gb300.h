@@ -131,6 +131,35 @@ dtfft_error_t dtfft_vgrid_get_nranks(dtfft_plan_t plan, int32_t* nranks);
 dtfft_error_t dtfft_vgrid_get_pencil(dtfft_plan_t plan, dtfft_layout_t layout, int32_t vrank,
                                      dtfft_pencil_t* pencil, size_t* offset);
 
+/* ------------------------------------------------------------------------ */
+/* Execute without allocating                                                */
+/* ------------------------------------------------------------------------ */
+
+/**
+ * dtfft_execute for callers that cannot allocate device memory.  No
+ * counterpart in the reference.
+ *
+ * dtfft_execute with aux = NULL allocates its scratch (dtfft_get_aux_bytes)
+ * with cudaMalloc on the first call.  Callers whose device memory belongs to
+ * another allocator (a framework's caching allocator, a fixed pool that
+ * forbids raw cudaMalloc) or that cannot take a first-use allocation and its
+ * possible device synchronisation use this entry point instead: it takes the
+ * scratch from a fixed 16 MiB buffer compiled into the library
+ * (dtfft_execute_noalloc_max_bytes) and calls no allocating routine.
+ *
+ * - Plans with dtfft_get_aux_bytes > 16 MiB are refused with
+ *   DTFFT_ERROR_NOALLOC_SCRATCH_TOO_SMALL.
+ * - The first call on a device looks the buffer's device address up
+ *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ * - Every call on a device shares the one buffer: calls whose kernels overlap
+ *   on the GPU (different streams without ordering) race on it.
+ * - Each GPU that loads this code holds the 16 MiB until the process exits.
+ */
+dtfft_error_t dtfft_execute_noalloc(dtfft_plan_t plan, void* in, void* out, dtfft_execute_t execute_type);
+
+/** Size in bytes of the fixed scratch buffer of dtfft_execute_noalloc. */
+size_t dtfft_execute_noalloc_max_bytes(void);
+
 /** Number of launches of this library's kernels since load (for benchmarks). */
 int64_t dtfft_gb_kernel_launch_count(void);
 
