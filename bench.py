@@ -273,6 +273,40 @@ def run_ours(args):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             e2e_ms = float(t.item())
 
+    # transpose-only cycle of the same grid (X->Y->Z->Y->X, executor NONE):
+    # 4 grid transposes per cycle, each one read + one write of the buffer
+    tonly = None
+    if not args.no_transpose_only:
+        tplan = dt.PlanC2C(DIMS, comm=comm, precision=dt.Precision.SINGLE, executor=dt.Executor.NONE,
+                           effort=dt.Effort(args.effort), config=dt.Config(stream=stream.cuda_stream))
+        dt.set_config(dt.Config())
+
+        def tstep():
+            tplan.execute(a, b, dt.Execute.FORWARD, aux)
+            tplan.execute(b, a, dt.Execute.BACKWARD, aux)
+
+        for _ in range(args.warmup):
+            tstep()
+        torch.cuda.synchronize()
+        L.dtfft_gb_profile_start()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        for _ in range(args.steps):
+            tstep()
+        g1.record(stream)
+        torch.cuda.synchronize()
+        L.dtfft_gb_profile_stop()
+        tprof = _profile_results(L)
+        t_ms = g0.elapsed_time(g1) / args.steps
+        tk = max(tprof, key=lambda r: r[2]) if tprof else ("none", 1, 0.0)
+        t_launch = tk[2] / max(tk[1], 1)
+        tonly = {"cycles_per_s": 1000.0 / t_ms, "ms_per_cycle": t_ms, "kernel": tk[0], "launch_ms": t_launch,
+                 "achieved_gbs": algo_bytes / (t_launch * 1e-3) / 1e9 if t_launch > 0 else 0.0,
+                 "frac": (algo_bytes / (t_launch * 1e-3) / 1e9) / peak if t_launch > 0 else 0.0,
+                 "effective_tbs": 4 * algo_bytes / (t_ms * 1e-3) / 1e12}
+        tplan.destroy()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -301,6 +335,7 @@ def run_ours(args):
             "gpu_launches": launches,
             "cpu_baseline": cpu,
             "clocks": clk,
+            "transpose_only": tonly,
         }
         print(json.dumps(line), flush=True)
     plan.destroy()
@@ -318,6 +353,7 @@ def main():
     ap.add_argument("--effort", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-transpose-only", action="store_true")
     ap.add_argument("--dims", type=int, nargs=3, default=None,
                     help="smaller C2C case for profiling (default: the 512^3 headline workload)")
     ap.add_argument("--grid", type=int, nargs=2, default=[2, 4])

@@ -35,37 +35,43 @@ box_transpose_kernel(const T* __restrict__ in, T* __restrict__ out,
     __shared__ T tile[TB][TA + 1];
     const i64 t = (i64)blockIdx.x;
     const int bi = nboxes > 1 ? find_box(boxes, nboxes, t) : 0;
-    const Box& bx = boxes[bi];
-    const i64 lt = t - bx.tile_begin;
-    const int per_c = bx.tiles_a * bx.tiles_b;
+    const Box* bp = boxes + bi;
+    const int tiles_a = __ldg(&bp->tiles_a);
+    const int per_c = tiles_a * __ldg(&bp->tiles_b);
+    const i64 lt = t - __ldg(&bp->tile_begin);
     const int c = (int)(lt / per_c);
     const int r = (int)(lt - (i64)c * per_c);
-    const int a0 = (r % bx.tiles_a) * TA;
-    const int b0 = (r / bx.tiles_a) * TB;
-    const int na = bx.na, nb = bx.nb;
+    const int a0 = (r % tiles_a) * TA;
+    const int b0 = (r / tiles_a) * TB;
     const int tx = threadIdx.x, ty = threadIdx.y;
-
-    const T* src = in + bx.src_off + (i64)c * bx.sc;
+    // in-tile extents; offsets inside a box fit 32 bits (checked when the list is built)
+    const int ra = min(TA, __ldg(&bp->na) - a0), rb = min(TB, __ldg(&bp->nb) - b0);
+    const int sb = (int)__ldg(&bp->sb), da = (int)__ldg(&bp->da_or_db);
+    const T* src = in + __ldg(&bp->src_off) + (i64)c * __ldg(&bp->sc) + a0 + (i64)b0 * sb;
+    T* dst = out + __ldg(&bp->dst_off) + (i64)c * __ldg(&bp->dc) + b0 + (i64)a0 * da;
+    if (ra == TA && rb == TB) {   // interior tile: no bounds checks
 #pragma unroll
-    for (int bb = ty; bb < TB; bb += ROWS) {
-        const int b = b0 + bb;
+        for (int bb = ty; bb < TB; bb += ROWS)
 #pragma unroll
-        for (int aa = tx; aa < TA; aa += 32) {
-            const int a = a0 + aa;
-            if (a < na && b < nb) tile[bb][aa] = src[a + (i64)b * bx.sb];
-        }
+            for (int aa = tx; aa < TA; aa += 32) tile[bb][aa] = src[aa + bb * sb];
+        __syncthreads();
+#pragma unroll
+        for (int aa = ty; aa < TA; aa += ROWS)
+#pragma unroll
+            for (int bb = tx; bb < TB; bb += 32) dst[bb + aa * da] = tile[bb][aa];
+        return;
     }
+#pragma unroll
+    for (int bb = ty; bb < TB; bb += ROWS)
+#pragma unroll
+        for (int aa = tx; aa < TA; aa += 32)
+            if (aa < ra && bb < rb) tile[bb][aa] = src[aa + bb * sb];
     __syncthreads();
-    T* dst = out + bx.dst_off + (i64)c * bx.dc;
 #pragma unroll
-    for (int aa = ty; aa < TA; aa += ROWS) {
-        const int a = a0 + aa;
+    for (int aa = ty; aa < TA; aa += ROWS)
 #pragma unroll
-        for (int bb = tx; bb < TB; bb += 32) {
-            const int b = b0 + bb;
-            if (a < na && b < nb) dst[b + (i64)a * bx.da_or_db] = tile[bb][aa];
-        }
-    }
+        for (int bb = tx; bb < TB; bb += 32)
+            if (aa < ra && bb < rb) dst[bb + aa * da] = tile[bb][aa];
 }
 
 // Copy boxes: the contiguous axis is the same on both sides, no staging.
@@ -101,6 +107,9 @@ dtfft_error_t boxes_upload(BoxList& bl) {
     std::vector<Box> kept;
     for (Box b : bl.host) {
         if (b.na <= 0 || b.nb <= 0 || b.nc <= 0) continue;
+        // in-tile offsets are 32-bit in the kernels
+        if ((i64)(TB + 1) * b.sb >= 0x7fffffffLL || (i64)(TA + 1) * b.da_or_db >= 0x7fffffffLL)
+            return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
         b.tiles_a = (b.na + TA - 1) / TA;
         b.tiles_b = (b.nb + TB - 1) / TB;
         b.tile_begin = tiles;
