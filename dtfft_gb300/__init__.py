@@ -19,7 +19,7 @@ import os
 from typing import Optional
 
 __all__ = [
-    "lib", "DtfftError", "Execute", "Transpose", "Layout", "Reshape", "Precision", "Effort",
+    "lib", "pencils_comm", "DtfftError", "Execute", "Transpose", "Layout", "Reshape", "Precision", "Effort",
     "Executor", "R2RKind", "Backend", "Platform", "Pencil", "Config", "set_config",
     "PlanC2C", "PlanR2C", "PlanR2R", "cart_comm", "world_comm", "COMM_WORLD",
 ]
@@ -190,6 +190,9 @@ def _declare(L):
     L.dtfft_vgrid_get_nranks.argtypes = [vp, P(i32)]
     L.dtfft_vgrid_cart_create.argtypes = [i32, P(i32), P(ctypes.c_int)]
     L.dtfft_vgrid_world_create.argtypes = [i32, P(ctypes.c_int)]
+    L.dtfft_vgrid_pencils_create.argtypes = [i32, i32, P(i32), P(i32), P(ctypes.c_int)]
+    L.dtfft_reshape_start.argtypes = [vp, vp, vp, ctypes.c_int, vp, P(vp)]
+    L.dtfft_reshape_end.argtypes = [vp, vp]
     L.dtfft_vgrid_free.argtypes = [P(ctypes.c_int)]
     L.dtfft_get_z_slab_enabled.argtypes = [vp, P(ctypes.c_bool)]
     L.dtfft_get_y_slab_enabled.argtypes = [vp, P(ctypes.c_bool)]
@@ -238,6 +241,19 @@ def world_comm(nprocs: int) -> int:
     """`nprocs` virtual ranks without a topology: the planner picks the grid."""
     h = ctypes.c_int()
     _check(lib().dtfft_vgrid_world_create(int(nprocs), ctypes.byref(h)), "dtfft_vgrid_world_create")
+    return h.value
+
+
+def pencils_comm(blocks) -> int:
+    """Virtual ranks that each own a block: `blocks[r] = (starts, counts)` in
+    dtfft_pencil_t order (dims[0] fastest).  Create the plan with
+    `Pencil(*blocks[0])` and this communicator."""
+    nd = len(blocks[0][0])
+    st = [int(v) for b in blocks for v in b[0]]
+    ct = [int(v) for b in blocks for v in b[1]]
+    h = ctypes.c_int()
+    _check(lib().dtfft_vgrid_pencils_create(len(blocks), nd, _dims_arr(st), _dims_arr(ct), ctypes.byref(h)),
+           "dtfft_vgrid_pencils_create")
     return h.value
 
 
@@ -341,6 +357,15 @@ class Plan:
 
     def reshape(self, input, output, reshape_type: Reshape, aux=None):
         _check(lib().dtfft_reshape(self._h, _ptr(input), _ptr(output), int(reshape_type), _ptr(aux)), "dtfft_reshape")
+
+    def reshape_start(self, input, output, reshape_type: Reshape, aux=None):
+        req = ctypes.c_void_p()
+        _check(lib().dtfft_reshape_start(self._h, _ptr(input), _ptr(output), int(reshape_type), _ptr(aux),
+                                         ctypes.byref(req)), "dtfft_reshape_start")
+        return req
+
+    def reshape_end(self, request):
+        _check(lib().dtfft_reshape_end(self._h, request), "dtfft_reshape_end")
 
     def report(self):
         _check(lib().dtfft_report(self._h), "dtfft_report")

@@ -103,6 +103,8 @@ struct VComm {
     int nprocs = 1;
     int ndims = 0;
     int dims[3] = {1, 1, 1};
+    int block_ndims = 0;                   // > 0: every rank's own block is registered
+    std::vector<int32_t> starts, counts;   // nprocs x block_ndims, Fortran order
 };
 static std::map<int, VComm> g_vcomms;
 static int g_next_comm = 0x4c000010;
@@ -129,10 +131,20 @@ VCommInfo comm_info(MPI_Comm comm) {
     return r;
 }
 
+bool comm_blocks(MPI_Comm comm, int* ndims, std::vector<int32_t>* starts, std::vector<int32_t>* counts) {
+    VComm v;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!lookup_comm(comm, v) || v.block_ndims == 0) return false;
+    *ndims = v.block_ndims;
+    *starts = v.starts;
+    *counts = v.counts;
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // Pencils
 // ---------------------------------------------------------------------------
-static void split(int n, int P, int r, int& start, int& count) {
+void split(int n, int P, int r, int& start, int& count) {
     // remainder to the last ranks (src/dtfft_pencil.F90:258-262)
     const int base = n / P, rem = n % P, first_big = P - rem;
     count = base + (r >= first_big ? 1 : 0);
@@ -141,7 +153,7 @@ static void split(int n, int P, int r, int& start, int& count) {
 
 // Global axis and grid-comm index of pencil dim d (get_permutations,
 // src/dtfft_transpose_plan.F90:1045-1082).
-static void perms(int ndims, int aligned, int* axes, int* comms) {
+void perms(int ndims, int aligned, int* axes, int* comms) {
     if (ndims == 2) {
         axes[0] = aligned == 1 ? 0 : 1; axes[1] = aligned == 1 ? 1 : 0;
         comms[0] = 0; comms[1] = 1;
@@ -171,6 +183,30 @@ Layout make_pencil_layout(int ndims, const int* gdims, const int* grid, int alig
             split(gdims[L.axes[d]], grid[cm], c[cm], L.r[r].start[d], L.r[r].count[d]);
             n *= L.r[r].count[d];
         }
+        for (int d = ndims; d < 3; ++d) { L.r[r].start[d] = 0; L.r[r].count[d] = 1; }
+        L.off[r] = off;
+        off += n;
+        L.max_local = std::max(L.max_local, n);
+    }
+    L.off[P] = off;
+    L.total = off;
+    for (int d = 0; d < ndims; ++d) L.gsize[d] = gdims[L.axes[d]];
+    return L;
+}
+
+Layout layout_from_boxes(int ndims, int aligned, const int* gdims, const std::vector<RankBox>& boxes) {
+    Layout L;
+    L.id = aligned;
+    L.nd = ndims;
+    int comms[3];
+    perms(ndims, aligned, L.axes, comms);
+    const int P = (int)boxes.size();
+    L.r = boxes;
+    L.off.resize(P + 1);
+    i64 off = 0;
+    for (int r = 0; r < P; ++r) {
+        i64 n = 1;
+        for (int d = 0; d < ndims; ++d) n *= L.r[r].count[d];
         for (int d = ndims; d < 3; ++d) { L.r[r].start[d] = 0; L.r[r].count[d] = 1; }
         L.off[r] = off;
         off += n;
@@ -280,6 +316,23 @@ int32_t dtfft_vgrid_cart_create(int32_t ndims, const int32_t* dims, MPI_Comm* co
         v.dims[i] = dims[i];
         v.nprocs *= dims[i];
     }
+    std::lock_guard<std::mutex> lk(g_mu);
+    const int h = g_next_comm++;
+    g_vcomms[h] = v;
+    *comm = (MPI_Comm)h;
+    return DTFFT_SUCCESS;
+}
+
+int32_t dtfft_vgrid_pencils_create(int32_t nprocs, int32_t ndims, const int32_t* starts, const int32_t* counts,
+                                   MPI_Comm* comm) {
+    if (!comm || !starts || !counts || nprocs < 1) return DTFFT_ERROR_INVALID_USAGE;
+    if (ndims != 2 && ndims != 3) return DTFFT_ERROR_PENCIL_NOT_INITIALIZED;
+    VComm v;
+    v.cart = false;
+    v.nprocs = nprocs;
+    v.block_ndims = ndims;
+    v.starts.assign(starts, starts + (size_t)nprocs * ndims);
+    v.counts.assign(counts, counts + (size_t)nprocs * ndims);
     std::lock_guard<std::mutex> lk(g_mu);
     const int h = g_next_comm++;
     g_vcomms[h] = v;

@@ -32,6 +32,11 @@ struct Plan {
     bool z_slab = false, y_slab = false;
     Layout pen[3];
     Layout real_x;              // R2C: real X pencils
+    bool user = false;          // built from every virtual rank's own block
+    bool reshape = false;       // the blocks split X: brick <-> pencil reshapes
+    bool final_reshape = false; // execute ends in / starts from Fourier-space bricks
+    Layout brick_x, brick_z;    // user bricks (real space), Fourier-space bricks
+    BoxList rs[4];              // reshape_type - DTFFT_RESHAPE_X_BRICKS_TO_PENCILS
     int elem = 8;               // bytes of a transposed element
     int real_elem = 4;          // bytes of a real element
     BoxList tr[7];              // index transpose_type + 3
@@ -46,6 +51,7 @@ struct Plan {
 
     ~Plan() {
         for (auto& b : tr) boxes_free(b);
+        for (auto& b : rs) boxes_free(b);
         for (auto*& f : fft) { delete f; f = nullptr; }
         for (auto*& f : ft) { delete f; f = nullptr; }
         if (aux) cudaFree(aux);
@@ -138,6 +144,25 @@ static dtfft_error_t build_transposes(Plan& p) {
     return DTFFT_SUCCESS;
 }
 
+// Brick <-> pencil moves (src/dtfft_reshape_plan.F90:338-367): X reshapes in
+// the real element for R2C, Z reshapes in the transformed element.
+static dtfft_error_t build_reshapes(Plan& p) {
+    if (!p.reshape) return DTFFT_SUCCESS;
+    const Layout& xp = p.kind == K_R2C ? p.real_x : p.pen[0];
+    const Layout& zp = p.pen[p.ndims - 1];
+    const int xe = p.kind == K_R2C ? p.real_elem : p.elem;
+    const Layout* from[4] = {&p.brick_x, &xp, &zp, &p.brick_z};
+    const Layout* to[4] = {&xp, &p.brick_x, &p.brick_z, &zp};
+    const int es[4] = {xe, xe, p.elem, p.elem};
+    for (int i = 0; i < 4; ++i) {
+        BoxList& bl = p.rs[i];
+        bl = make_boxes(*from[i], *to[i], es[i]);
+        bl.cfg = default_tile(es[i]);
+        GB_TRY(boxes_upload(bl));
+    }
+    return DTFFT_SUCCESS;
+}
+
 // FFT plans per aligned dim (src/dtfft_plan.F90:2381-2653)
 static dtfft_error_t build_ffts(Plan& p) {
     if (p.transpose_only) return DTFFT_SUCCESS;
@@ -205,7 +230,7 @@ static void build_fused(Plan& p) {
 
 static dtfft_error_t create_plan(int kind, int8_t ndims, const int32_t* dims, const int32_t* kinds,
                                  MPI_Comm comm, dtfft_precision_t precision, dtfft_effort_t effort,
-                                 dtfft_executor_t executor, dtfft_plan_t* out) {
+                                 dtfft_executor_t executor, dtfft_plan_t* out, const UserGeometry* ug = nullptr) {
     if (!out) return DTFFT_ERROR_INVALID_USAGE;
     *out = nullptr;
     // check_create_args order (src/dtfft_plan.F90:2107-2219)
@@ -238,10 +263,30 @@ static dtfft_error_t create_plan(int kind, int8_t ndims, const int32_t* dims, co
     p->real_elem = real;
     p->elem = kind == K_R2R ? real : 2 * real;
 
-    dtfft_error_t e = choose_grid(*p, vc, cfg.enable_z_slab, cfg.enable_y_slab);
+    dtfft_error_t e = DTFFT_SUCCESS;
+    if (ug) {
+        // every rank's own block (src/dtfft_plan.F90:2014-2089)
+        p->user = true;
+        for (int i = 0; i < 3; ++i) p->grid[i] = ug->grid[i];
+        p->P = (int)ug->pen[0].r.size();
+        p->z_slab = ug->z_slab;
+        p->y_slab = ug->y_slab;
+        for (int d = 0; d < ndims; ++d) p->pen[d] = ug->pen[d];
+        if (kind == K_R2C) p->real_x = ug->real_x;
+        p->reshape = ug->reshape;
+        if (p->reshape) {
+            p->brick_x = ug->brick_x;
+            p->brick_z = ug->brick_z;
+            p->final_reshape = ug->final_grid > 1 && cfg.enable_fourier_reshape && !p->z_slab;
+        }
+    } else {
+        e = choose_grid(*p, vc, cfg.enable_z_slab, cfg.enable_y_slab);
+        if (e == DTFFT_SUCCESS) {
+            for (int d = 0; d < ndims; ++d) p->pen[d] = make_pencil_layout(ndims, p->tdims, p->grid, d + 1);
+            if (kind == K_R2C) p->real_x = make_pencil_layout(ndims, p->dims, p->grid, 1);
+        }
+    }
     if (e == DTFFT_SUCCESS) {
-        for (int d = 0; d < ndims; ++d) p->pen[d] = make_pencil_layout(ndims, p->tdims, p->grid, d + 1);
-        if (kind == K_R2C) p->real_x = make_pencil_layout(ndims, p->dims, p->grid, 1);
         if (kind == K_R2R && !tonly && !kinds) e = DTFFT_ERROR_MISSING_R2R_KINDS;
         if (kind == K_R2R && !tonly && executor == DTFFT_EXECUTOR_CUFFT) e = DTFFT_ERROR_R2R_FFT_NOT_SUPPORTED;
     }
@@ -253,6 +298,7 @@ static dtfft_error_t create_plan(int kind, int8_t ndims, const int32_t* dims, co
         else e = DTFFT_ERROR_GPU_CALL_FAILED;
     }
     if (e == DTFFT_SUCCESS) e = build_transposes(*p);
+    if (e == DTFFT_SUCCESS) e = build_reshapes(*p);
     if (e == DTFFT_SUCCESS) e = build_ffts(*p);
     if (e == DTFFT_SUCCESS) build_fused(*p);
     if (e == DTFFT_SUCCESS && (effort == DTFFT_EXHAUSTIVE || cfg.enable_kernel_autotune)) {
@@ -305,8 +351,91 @@ static dtfft_error_t F(Plan& p, int d, const void* in, void* out, int sign) {
     return f->execute(in, out, sign, p.stream);
 }
 
+static dtfft_error_t RS(Plan& p, int type, const void* in, void* out) {
+    return boxes_launch(p.rs[type - DTFFT_RESHAPE_X_BRICKS_TO_PENCILS], in, out, p.stream);
+}
+
+// execute_2d_reshape / execute_z_slab_reshape / execute_generic_reshape
+// (src/dtfft_plan.F90:915-966,1018-1048,1103-1162), with their buffer roles.
+static dtfft_error_t run_execute_reshape(Plan& p, void* in, void* out, bool fwd, void* aux) {
+    const int S = fwd ? FFT_FWD : FFT_BWD;
+    const int XB2P = DTFFT_RESHAPE_X_BRICKS_TO_PENCILS, XP2B = DTFFT_RESHAPE_X_PENCILS_TO_BRICKS;
+    const int ZP2B = DTFFT_RESHAPE_Z_PENCILS_TO_BRICKS, ZB2P = DTFFT_RESHAPE_Z_BRICKS_TO_PENCILS;
+    const bool fin = p.final_reshape;
+    if (p.ndims == 2 || p.y_slab) {
+        if (p.transpose_only) {
+            if (fwd) {
+                GB_TRY(RS(p, XB2P, in, aux));
+                if (fin) { GB_TRY(T(p, 1, aux, in)); return RS(p, ZP2B, in, out); }
+                return T(p, 1, aux, out);
+            }
+            if (fin) { GB_TRY(RS(p, ZB2P, in, out)); GB_TRY(T(p, -1, out, aux)); }
+            else GB_TRY(T(p, -1, in, aux));
+            return RS(p, XP2B, aux, out);
+        }
+        if (fwd) {
+            GB_TRY(RS(p, XB2P, in, aux));
+            GB_TRY(F(p, 1, aux, out, S));
+            GB_TRY(T(p, 1, out, aux));
+            if (fin) { GB_TRY(F(p, 2, aux, aux, S)); return RS(p, ZP2B, aux, out); }
+            return F(p, 2, aux, out, S);
+        }
+        if (fin) { GB_TRY(RS(p, ZB2P, in, aux)); GB_TRY(F(p, 2, aux, aux, S)); }
+        else GB_TRY(F(p, 2, in, aux, S));
+        GB_TRY(T(p, -1, aux, in));
+        GB_TRY(F(p, 1, in, aux, S));
+        return RS(p, XP2B, aux, out);
+    }
+    if (p.z_slab) {
+        if (p.transpose_only) {
+            if (fwd) { GB_TRY(RS(p, XB2P, in, aux)); return T(p, 3, aux, out); }
+            GB_TRY(T(p, -3, in, aux));
+            return RS(p, XP2B, aux, out);
+        }
+        if (fwd) {
+            GB_TRY(RS(p, XB2P, in, aux));
+            GB_TRY(F(p, 1, aux, in, S));
+            GB_TRY(T(p, 3, in, aux));
+            return F(p, 3, aux, out, S);
+        }
+        GB_TRY(F(p, 3, in, aux, S));
+        GB_TRY(T(p, -3, aux, in));
+        GB_TRY(F(p, 1, in, aux, S));
+        return RS(p, XP2B, aux, out);
+    }
+    if (p.transpose_only) {
+        if (fwd) {
+            GB_TRY(RS(p, XB2P, in, aux));
+            GB_TRY(T(p, 1, aux, in));
+            if (fin) { GB_TRY(T(p, 2, in, aux)); return RS(p, ZP2B, aux, out); }
+            return T(p, 2, in, out);
+        }
+        if (fin) { GB_TRY(RS(p, ZB2P, in, aux)); GB_TRY(T(p, -2, aux, out)); }
+        else GB_TRY(T(p, -2, in, out));
+        GB_TRY(T(p, -1, out, aux));
+        return RS(p, XP2B, aux, out);
+    }
+    if (fwd) {
+        GB_TRY(RS(p, XB2P, in, aux));
+        GB_TRY(F(p, 1, aux, out, S));
+        GB_TRY(T(p, 1, out, aux));
+        GB_TRY(F(p, 2, aux, aux, S));
+        GB_TRY(T(p, 2, aux, out));
+        if (fin) { GB_TRY(F(p, 3, out, aux, S)); return RS(p, ZP2B, aux, out); }
+        return F(p, 3, out, out, S);
+    }
+    if (fin) { GB_TRY(RS(p, ZB2P, in, aux)); GB_TRY(F(p, 3, aux, in, S)); }
+    else GB_TRY(F(p, 3, in, in, S));
+    GB_TRY(T(p, -2, in, aux));
+    GB_TRY(F(p, 2, aux, aux, S));
+    GB_TRY(T(p, -1, aux, in));
+    GB_TRY(F(p, 1, in, aux, S));
+    return RS(p, XP2B, aux, out);
+}
+
 // execute_2d / execute_z_slab / execute_generic (src/dtfft_plan.F90:877-1101)
 static dtfft_error_t run_execute(Plan& p, void* in, void* out, bool fwd, void* aux, bool inplace) {
+    if (p.reshape) return run_execute_reshape(p, in, out, fwd, aux);
     const int S = fwd ? FFT_FWD : FFT_BWD;
     if (p.ndims == 2 || p.y_slab) {
         if (p.transpose_only) return T(p, fwd ? 1 : -1, in, out);
@@ -400,29 +529,46 @@ static dtfft_error_t pencil_dims(const dtfft_pencil_t* pencil, MPI_Comm comm, in
     return DTFFT_SUCCESS;
 }
 
-dtfft_error_t dtfft_create_plan_c2c_pencil(const dtfft_pencil_t* pencil, MPI_Comm comm, dtfft_precision_t precision,
-                                           dtfft_effort_t effort, dtfft_executor_t executor, dtfft_plan_t* plan) {
+// Virtual ranks with their own blocks (dtfft_vgrid_pencils_create): the
+// calling process plays virtual rank 0, so `pencil` is rank 0's block; the
+// plan covers every rank (src/dtfft_plan.F90:2014-2089).
+static dtfft_error_t create_user_plan(int kind, const dtfft_pencil_t* pencil, const int32_t* kinds, MPI_Comm comm,
+                                      dtfft_precision_t precision, dtfft_effort_t effort, dtfft_executor_t executor,
+                                      dtfft_plan_t* plan) {
     if (!plan) return DTFFT_ERROR_INVALID_USAGE;
+    if (!pencil) return DTFFT_ERROR_INVALID_USAGE;
+    if (pencil->ndims != 2 && pencil->ndims != 3) return DTFFT_ERROR_PENCIL_NOT_INITIALIZED;
+    int bnd = 0;
+    std::vector<int32_t> st, ct;
+    if (comm_blocks(comm, &bnd, &st, &ct)) {
+        if (bnd != pencil->ndims) return DTFFT_ERROR_PENCIL_ARRAYS_SIZE_MISMATCH;
+        for (int d = 0; d < bnd; ++d)
+            if (pencil->starts[d] != st[d] || pencil->counts[d] != ct[d]) return DTFFT_ERROR_PENCIL_SHAPE_MISMATCH;
+        const int P = (int)(st.size() / bnd);
+        UserGeometry g;
+        const dtfft_config_t& cfg = config();
+        GB_TRY(user_geometry(bnd, P, st.data(), ct.data(), kind == K_R2C, cfg.enable_z_slab, cfg.enable_y_slab, g));
+        return create_plan(kind, (int8_t)bnd, g.dims, kinds, comm, precision, effort, executor, plan, &g);
+    }
     int32_t dims[3];
     GB_TRY(pencil_dims(pencil, comm, dims));
-    return create_plan(K_C2C, pencil->ndims, dims, nullptr, comm, precision, effort, executor, plan);
+    return create_plan(kind, pencil->ndims, dims, kinds, comm, precision, effort, executor, plan);
+}
+
+dtfft_error_t dtfft_create_plan_c2c_pencil(const dtfft_pencil_t* pencil, MPI_Comm comm, dtfft_precision_t precision,
+                                           dtfft_effort_t effort, dtfft_executor_t executor, dtfft_plan_t* plan) {
+    return create_user_plan(K_C2C, pencil, nullptr, comm, precision, effort, executor, plan);
 }
 
 dtfft_error_t dtfft_create_plan_r2c_pencil(const dtfft_pencil_t* pencil, MPI_Comm comm, dtfft_precision_t precision,
                                            dtfft_effort_t effort, dtfft_executor_t executor, dtfft_plan_t* plan) {
-    if (!plan) return DTFFT_ERROR_INVALID_USAGE;
-    int32_t dims[3];
-    GB_TRY(pencil_dims(pencil, comm, dims));
-    return create_plan(K_R2C, pencil->ndims, dims, nullptr, comm, precision, effort, executor, plan);
+    return create_user_plan(K_R2C, pencil, nullptr, comm, precision, effort, executor, plan);
 }
 
 dtfft_error_t dtfft_create_plan_r2r_pencil(const dtfft_pencil_t* pencil, const dtfft_r2r_kind_t* kinds, MPI_Comm comm,
                                            dtfft_precision_t precision, dtfft_effort_t effort,
                                            dtfft_executor_t executor, dtfft_plan_t* plan) {
-    if (!plan) return DTFFT_ERROR_INVALID_USAGE;
-    int32_t dims[3];
-    GB_TRY(pencil_dims(pencil, comm, dims));
-    return create_plan(K_R2R, pencil->ndims, dims, (const int32_t*)kinds, comm, precision, effort, executor, plan);
+    return create_user_plan(K_R2R, pencil, (const int32_t*)kinds, comm, precision, effort, executor, plan);
 }
 
 dtfft_error_t dtfft_destroy(dtfft_plan_t* plan) {
@@ -442,7 +588,8 @@ dtfft_error_t dtfft_execute(dtfft_plan_t plan, void* in, void* out, dtfft_execut
     if (execute_type != DTFFT_EXECUTE_FORWARD && execute_type != DTFFT_EXECUTE_BACKWARD)
         return DTFFT_ERROR_INVALID_EXECUTE_TYPE;
     const bool inplace = in == out;
-    if (p->transpose_only && inplace && (p->ndims == 2 || p->y_slab)) return DTFFT_ERROR_INPLACE_TRANSPOSE;
+    if (p->transpose_only && inplace && (p->ndims == 2 || p->y_slab || (p->reshape && !p->final_reshape)))
+        return DTFFT_ERROR_INPLACE_TRANSPOSE;
     if (aux && (aux == in || aux == out)) return DTFFT_ERROR_INVALID_AUX;
     if (p->transpose_only && p->kind == K_R2C) return DTFFT_ERROR_R2C_EXECUTE_CALLED;
     GB_TRY(check_ptrs(in, out, aux));
@@ -465,7 +612,8 @@ dtfft_error_t execute_into_scratch(dtfft_plan_t plan, void* in, void* out, int e
     if (execute_type != DTFFT_EXECUTE_FORWARD && execute_type != DTFFT_EXECUTE_BACKWARD)
         return DTFFT_ERROR_INVALID_EXECUTE_TYPE;
     const bool inplace = in == out;
-    if (p->transpose_only && inplace && (p->ndims == 2 || p->y_slab)) return DTFFT_ERROR_INPLACE_TRANSPOSE;
+    if (p->transpose_only && inplace && (p->ndims == 2 || p->y_slab || (p->reshape && !p->final_reshape)))
+        return DTFFT_ERROR_INPLACE_TRANSPOSE;
     if (p->transpose_only && p->kind == K_R2C) return DTFFT_ERROR_R2C_EXECUTE_CALLED;
     if (needed) *needed = p->alloc_bytes();
     if (p->alloc_bytes() > scratch_bytes) return DTFFT_ERROR_NOALLOC_SCRATCH_TOO_SMALL;
@@ -511,31 +659,52 @@ dtfft_error_t dtfft_transpose_end(dtfft_plan_t plan, dtfft_request_t request) {
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
     Request* r = reinterpret_cast<Request*>(request);
     if (!r || r->magic != kReqMagic) return DTFFT_ERROR_INVALID_REQUEST;
+    if (r->type >= DTFFT_RESHAPE_X_BRICKS_TO_PENCILS) return DTFFT_ERROR_INVALID_REQUEST;
     r->magic = 0;
     delete r;
     return DTFFT_SUCCESS;
 }
 
+// reshape_private checks (src/dtfft_plan.F90:508-537)
+static dtfft_error_t reshape_checks(Plan* p, void* in, void* out, int t, void* aux) {
+    if (t < DTFFT_RESHAPE_X_BRICKS_TO_PENCILS || t > DTFFT_RESHAPE_Z_BRICKS_TO_PENCILS)
+        return DTFFT_ERROR_INVALID_RESHAPE_TYPE;
+    if (in == out) return DTFFT_ERROR_INPLACE_RESHAPE;
+    if (!p->reshape) return DTFFT_ERROR_RESHAPE_NOT_SUPPORTED;
+    if (aux && (aux == in || aux == out)) return DTFFT_ERROR_INVALID_AUX;
+    return check_ptrs(in, out, aux);
+}
+
 dtfft_error_t dtfft_reshape(dtfft_plan_t plan, void* in, void* out, dtfft_reshape_t reshape_type, void* aux) {
-    (void)in; (void)out; (void)aux;
+    if (!in || !out) return DTFFT_ERROR_INVALID_USAGE;
     Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
-    if (reshape_type < DTFFT_RESHAPE_X_BRICKS_TO_PENCILS || reshape_type > DTFFT_RESHAPE_Z_BRICKS_TO_PENCILS)
-        return DTFFT_ERROR_INVALID_RESHAPE_TYPE;
-    return DTFFT_ERROR_RESHAPE_NOT_SUPPORTED;
+    GB_TRY(reshape_checks(p, in, out, (int)reshape_type, aux));
+    return RS(*p, (int)reshape_type, in, out);
 }
 
 dtfft_error_t dtfft_reshape_start(dtfft_plan_t plan, void* in, void* out, dtfft_reshape_t reshape_type, void* aux,
                                   dtfft_request_t* request) {
-    if (!request) return DTFFT_ERROR_INVALID_USAGE;
-    return dtfft_reshape(plan, in, out, reshape_type, aux);
+    if (!in || !out || !request) return DTFFT_ERROR_INVALID_USAGE;
+    Plan* p = as_plan(plan);
+    if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
+    GB_TRY(reshape_checks(p, in, out, (int)reshape_type, aux));
+    // one copy kernel on the plan stream; the request only records it
+    GB_TRY(RS(*p, (int)reshape_type, in, out));
+    Request* r = new Request{kReqMagic, (int)reshape_type};
+    *request = r;
+    return DTFFT_SUCCESS;
 }
 
 dtfft_error_t dtfft_reshape_end(dtfft_plan_t plan, dtfft_request_t request) {
     Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
-    (void)request;
-    return DTFFT_ERROR_RESHAPE_NOT_ACTIVE;
+    Request* r = reinterpret_cast<Request*>(request);
+    if (!r || r->magic != kReqMagic) return DTFFT_ERROR_INVALID_REQUEST;
+    if (r->type < DTFFT_RESHAPE_X_BRICKS_TO_PENCILS) return DTFFT_ERROR_INVALID_REQUEST;
+    r->magic = 0;
+    delete r;
+    return DTFFT_SUCCESS;
 }
 
 dtfft_error_t dtfft_get_z_slab_enabled(dtfft_plan_t plan, bool* v) {
@@ -618,15 +787,19 @@ dtfft_error_t dtfft_get_aux_size_transpose(dtfft_plan_t plan, size_t* s) {
     *s = 0; return DTFFT_SUCCESS;
 }
 
+// A reshape is one copy kernel from `in` to `out`: no workspace
+// (src/dtfft_plan.F90:1436-1451 reports the exchange backend's).
 dtfft_error_t dtfft_get_aux_bytes_reshape(dtfft_plan_t plan, size_t* b) {
     if (!b) return DTFFT_ERROR_INVALID_USAGE;
     Plan* p = as_plan(plan); if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
+    if (!p->reshape) return DTFFT_ERROR_RESHAPE_NOT_SUPPORTED;
     *b = 0; return DTFFT_SUCCESS;
 }
 
 dtfft_error_t dtfft_get_aux_size_reshape(dtfft_plan_t plan, size_t* s) {
     if (!s) return DTFFT_ERROR_INVALID_USAGE;
     Plan* p = as_plan(plan); if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
+    if (!p->reshape) return DTFFT_ERROR_RESHAPE_NOT_SUPPORTED;
     *s = 0; return DTFFT_SUCCESS;
 }
 
@@ -636,10 +809,12 @@ dtfft_error_t dtfft_get_pencil(dtfft_plan_t plan, dtfft_layout_t layout, dtfft_p
     if (layout < DTFFT_LAYOUT_X_BRICKS || layout > DTFFT_LAYOUT_Z_BRICKS) return DTFFT_ERROR_INVALID_LAYOUT;
     const Layout* L = nullptr;
     switch (layout) {
+    case DTFFT_LAYOUT_X_BRICKS: if (p->reshape) L = &p->brick_x; break;
     case DTFFT_LAYOUT_X_PENCILS: L = p->kind == K_R2C ? &p->real_x : &p->pen[0]; break;
     case DTFFT_LAYOUT_X_PENCILS_FOURIER: if (p->kind == K_R2C) L = &p->pen[0]; break;
     case DTFFT_LAYOUT_Y_PENCILS: L = &p->pen[1]; break;
     case DTFFT_LAYOUT_Z_PENCILS: if (p->ndims == 3) L = &p->pen[2]; break;
+    case DTFFT_LAYOUT_Z_BRICKS: if (p->reshape) L = &p->brick_z; break;
     default: break;
     }
     if (!L) return DTFFT_ERROR_INVALID_LAYOUT;
@@ -666,10 +841,12 @@ dtfft_error_t dtfft_vgrid_get_pencil(dtfft_plan_t plan, dtfft_layout_t layout, i
     if (vrank < 0 || vrank >= p->P) return DTFFT_ERROR_INVALID_USAGE;
     const Layout* L = nullptr;
     switch (layout) {
+    case DTFFT_LAYOUT_X_BRICKS: if (p->reshape) L = &p->brick_x; break;
     case DTFFT_LAYOUT_X_PENCILS: L = p->kind == K_R2C ? &p->real_x : &p->pen[0]; break;
     case DTFFT_LAYOUT_X_PENCILS_FOURIER: if (p->kind == K_R2C) L = &p->pen[0]; break;
     case DTFFT_LAYOUT_Y_PENCILS: L = &p->pen[1]; break;
     case DTFFT_LAYOUT_Z_PENCILS: if (p->ndims == 3) L = &p->pen[2]; break;
+    case DTFFT_LAYOUT_Z_BRICKS: if (p->reshape) L = &p->brick_z; break;
     default: break;
     }
     if (!L) return DTFFT_ERROR_INVALID_LAYOUT;

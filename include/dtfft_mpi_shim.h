@@ -58,6 +58,29 @@ int32_t dtfft_vgrid_cart_create(int32_t ndims, const int32_t* dims, MPI_Comm* co
  */
 int32_t dtfft_vgrid_world_create(int32_t nprocs, MPI_Comm* comm);
 
+/**
+ * Creates a handle for `nprocs` virtual ranks without a topology, each owning
+ * its own block of the global domain: what `nprocs` MPI processes that each
+ * pass their dtfft_pencil_t to dtfft_create_plan_*_pencil describe together
+ * (dtfft_plan.F90:2014-2089 and dtfft_pencil.F90:777-908 of the reference).
+ *
+ * @param[in]  nprocs  number of virtual ranks
+ * @param[in]  ndims   2 or 3
+ * @param[in]  starts  nprocs x ndims block starts, rank-major, in the order of
+ *                     dtfft_pencil_t::starts (dims[0] is the fastest axis)
+ * @param[in]  counts  nprocs x ndims block counts, same order
+ * @param[out] comm    handle to pass to dtfft_create_plan_*_pencil together
+ *                     with virtual rank 0's block
+ *
+ * The blocks are checked when the plan is created, with the reference's error
+ * codes (DTFFT_ERROR_PENCIL_*).  Blocks that split the fastest axis are bricks:
+ * the plan then provides dtfft_reshape between them and X pencils, and
+ * dtfft_execute starts from (and returns to) the bricks.  Virtual rank r's
+ * block of any layout sits at the offset dtfft_vgrid_get_pencil reports.
+ */
+int32_t dtfft_vgrid_pencils_create(int32_t nprocs, int32_t ndims, const int32_t* starts, const int32_t* counts,
+                                   MPI_Comm* comm);
+
 /** Releases a handle made by dtfft_vgrid_cart_create or dtfft_vgrid_world_create. */
 int32_t dtfft_vgrid_free(MPI_Comm* comm);
 
