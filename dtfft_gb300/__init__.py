@@ -19,7 +19,7 @@ import os
 from typing import Optional
 
 __all__ = [
-    "lib", "pencils_comm", "DtfftError", "Execute", "Transpose", "Layout", "Reshape", "Precision", "Effort",
+    "lib", "pencils_comm", "Batch", "DtfftError", "Execute", "Transpose", "Layout", "Reshape", "Precision", "Effort",
     "Executor", "R2RKind", "Backend", "Platform", "Pencil", "Config", "set_config",
     "PlanC2C", "PlanR2C", "PlanR2R", "cart_comm", "world_comm", "COMM_WORLD",
 ]
@@ -216,6 +216,10 @@ def _declare(L):
     L.gb_fft_create.argtypes = [i32, i32, i32, i32, i32, i32, P(i32), P(i32), P(i32), P(i32), vp, P(vp)]
     L.gb_fft_execute.argtypes = [vp, vp, vp, i32]
     L.gb_fft_destroy.argtypes = [P(vp)]
+    L.dtfft_gb_batch_create.argtypes = [i32, P(vp), i32, P(vp)]
+    L.dtfft_gb_batch_execute.argtypes = [vp, P(vp), P(vp), P(vp), ctypes.c_int, vp]
+    L.dtfft_gb_batch_graph_nodes.argtypes = [vp, P(ctypes.c_int64)]
+    L.dtfft_gb_batch_destroy.argtypes = [P(vp)]
     for name in dir(L):
         pass
 
@@ -530,3 +534,35 @@ class PlanR2R(Plan):
             h = _create("dtfft_create_plan_r2r", len(d), _dims_arr(d), k, int(comm), int(precision), int(effort),
                         int(executor))
         super().__init__(h)
+
+
+class Batch:
+    """Several plans executed with one CUDA graph launch (dtfft_gb_batch_*)."""
+
+    def __init__(self, plans, lanes: int = 0):
+        self._plans = list(plans)
+        arr = (ctypes.c_void_p * len(self._plans))(*[p._h.value if isinstance(p._h, ctypes.c_void_p) else p._h
+                                                       for p in self._plans])
+        h = ctypes.c_void_p()
+        _check(lib().dtfft_gb_batch_create(len(self._plans), arr, int(lanes), ctypes.byref(h)),
+               "dtfft_gb_batch_create")
+        self._h = h
+
+    def execute(self, inputs, outputs, execute_type: Execute, auxs=None, stream=None):
+        n = len(self._plans)
+        ins = (ctypes.c_void_p * n)(*[_ptr(x) for x in inputs])
+        outs = (ctypes.c_void_p * n)(*[_ptr(x) for x in outputs])
+        ax = (ctypes.c_void_p * n)(*[_ptr(x) for x in auxs]) if auxs is not None else None
+        s = None if stream is None else int(getattr(stream, "cuda_stream", stream))
+        _check(lib().dtfft_gb_batch_execute(self._h, ins, outs, ax, int(execute_type), s), "dtfft_gb_batch_execute")
+
+    @property
+    def graph_nodes(self) -> int:
+        v = ctypes.c_int64()
+        _check(lib().dtfft_gb_batch_graph_nodes(self._h, ctypes.byref(v)), "dtfft_gb_batch_graph_nodes")
+        return int(v.value)
+
+    def destroy(self):
+        if self._h:
+            _check(lib().dtfft_gb_batch_destroy(ctypes.byref(self._h)), "dtfft_gb_batch_destroy")
+            self._h = None

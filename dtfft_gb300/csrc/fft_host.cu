@@ -181,6 +181,29 @@ static const size_t kSmemBudget = 96 * 1024;
 // Fill geometry, tables and launch shape of one step.
 static int pipe_occupancy(int dbl, int m, int E, bool fused, int threads, size_t smem);
 
+// Kernel attributes are set when a plan is built, never on the launch path:
+// execute then only enqueues kernels (and can be captured into a CUDA graph).
+static dtfft_error_t set_smem_attrs(const void* fn, size_t smem) {
+    if (!fn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    if (smem > 48 * 1024) GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // favour shared memory over L1 so several CTAs fit per SM
+    GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared));
+    return DTFFT_SUCCESS;
+}
+
+static int sm_count();
+
+static dtfft_error_t prepare_launch(const FftStep& S) {
+    (void)sm_count();
+    (void)status_ptr();
+    const void* fn;
+    if (S.E) fn = S.dbl ? (const void*)KPtr<double>::reg(S.E, S.cols, S.mode == M_C2C)
+                        : (const void*)KPtr<float>::reg(S.E, S.cols, S.mode == M_C2C);
+    else fn = S.dbl ? (const void*)KPtr<double>::generic(S.cols) : (const void*)KPtr<float>::generic(S.cols);
+    return set_smem_attrs(fn, S.smem);
+}
+
 static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
     int m, sign;
     if (!mode_geometry(S.mode, S.n, S.sign, m, sign)) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
@@ -247,7 +270,7 @@ tables:
     } break;
     default: break;
     }
-    return DTFFT_SUCCESS;
+    return prepare_launch(S);
 }
 
 template <typename R, bool FUSED>
@@ -325,16 +348,9 @@ static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, 
         const bool c2c = S.mode == M_C2C;
         void (*kfn)(Args<R>) = (void (*)(Args<R>))KPtr<R>::reg(S.E, COLS, c2c);
         if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-        if (S.smem > 48 * 1024)
-            GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
-        // favour shared memory over L1 so several CTAs fit per SM
-        GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                         (int)cudaSharedmemCarveoutMaxShared));
         kfn<<<(unsigned)ctas, S.threads, S.smem, s>>>(A);
     } else {
         void (*gfn)(Args<R>) = (void (*)(Args<R>))KPtr<R>::generic(COLS);
-        if (S.smem > 48 * 1024)
-            GB_CUDA_TRY(cudaFuncSetAttribute(gfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
         gfn<<<(unsigned)ctas, 256, S.smem, s>>>(A);
     }
     if (tok) {
@@ -537,6 +553,11 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, FusedFT** out) 
         if (ds) p->owned_.push_back(ds);
         p->groups_ = dg; p->segs_ = ds;
     }
+    if (err == DTFFT_SUCCESS) {
+        (void)sm_count();
+        (void)status_ptr();
+        err = set_smem_attrs(dbl ? (const void*)KPtr<double>::xpose(E) : (const void*)KPtr<float>::xpose(E), p->smem_);
+    }
     if (err != DTFFT_SUCCESS) { delete p; return err; }
     *out = p;
     return DTFFT_SUCCESS;
@@ -557,10 +578,6 @@ static dtfft_error_t launch_fused_t(const FusedFT& F, int m, int E, int T, int S
     for (int i = 0; i < A.st.ns; ++i) A.st.radix[i] = sch.radix[i];
     void (*kfn)(FArgs<R>) = (void (*)(FArgs<R>))KPtr<R>::xpose(E);
     if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-    if (smem > 48 * 1024)
-        GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    GB_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                     (int)cudaSharedmemCarveoutMaxShared));
     void* tok = prof_begin(s);
     kfn<<<(unsigned)ctas, S * T, smem, s>>>(A);
     if (tok) prof_end(tok, std::string("fftxpose_m") + std::to_string(m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);

@@ -581,9 +581,9 @@ dtfft_error_t dtfft_destroy(dtfft_plan_t* plan) {
     return DTFFT_SUCCESS;
 }
 
-dtfft_error_t dtfft_execute(dtfft_plan_t plan, void* in, void* out, dtfft_execute_t execute_type, void* aux) {
+// execute_private checks (src/dtfft_plan.F90:780-835)
+static dtfft_error_t execute_checks(Plan* p, void* in, void* out, int execute_type, void* aux) {
     if (!in || !out) return DTFFT_ERROR_INVALID_USAGE;
-    Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
     if (execute_type != DTFFT_EXECUTE_FORWARD && execute_type != DTFFT_EXECUTE_BACKWARD)
         return DTFFT_ERROR_INVALID_EXECUTE_TYPE;
@@ -592,10 +592,15 @@ dtfft_error_t dtfft_execute(dtfft_plan_t plan, void* in, void* out, dtfft_execut
         return DTFFT_ERROR_INPLACE_TRANSPOSE;
     if (aux && (aux == in || aux == out)) return DTFFT_ERROR_INVALID_AUX;
     if (p->transpose_only && p->kind == K_R2C) return DTFFT_ERROR_R2C_EXECUTE_CALLED;
-    GB_TRY(check_ptrs(in, out, aux));
+    return check_ptrs(in, out, aux);
+}
+
+dtfft_error_t dtfft_execute(dtfft_plan_t plan, void* in, void* out, dtfft_execute_t execute_type, void* aux) {
+    Plan* p = as_plan(plan);
+    GB_TRY(execute_checks(p, in, out, (int)execute_type, aux));
     void* a = nullptr;
     GB_TRY(get_aux(*p, aux, &a));
-    return run_execute(*p, in, out, execute_type == DTFFT_EXECUTE_FORWARD, a, inplace);
+    return run_execute(*p, in, out, execute_type == DTFFT_EXECUTE_FORWARD, a, in == out);
 }
 
 }  // extern "C"
@@ -952,6 +957,163 @@ dtfft_error_t dtfft_get_reshape_backend(dtfft_plan_t plan, dtfft_backend_t* b) {
     if (!b) return DTFFT_ERROR_INVALID_USAGE;
     Plan* p = as_plan(plan); if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
     *b = DTFFT_BACKEND_NONE; return DTFFT_SUCCESS;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batches: many plans executed as one CUDA graph.  The reference has no
+// batching API; a caller of it runs one dtfft_execute per plan.  Here every
+// plan's schedule is captured once on its own branch of a graph (plans spread
+// over `lanes` streams, so the kernels of small transforms run side by side)
+// and later calls replay the graph with one launch.
+// ===========================================================================
+namespace gb {
+
+static const uint32_t kBatchMagic = 0x47424254u;   // "GBBT"
+
+struct Batch {
+    uint32_t magic = kBatchMagic;
+    std::vector<Plan*> plans;
+    std::vector<cudaStream_t> lanes;
+    cudaStream_t cap = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> joins;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<const void*> key;   // type, then in/out/aux of every plan
+    size_t nodes = 0;
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr; graph = nullptr; nodes = 0;
+        key.clear();
+    }
+    ~Batch() {
+        drop_graph();
+        for (auto l : lanes) cudaStreamDestroy(l);
+        for (auto e : joins) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        if (cap) cudaStreamDestroy(cap);
+        magic = 0;
+    }
+};
+
+static Batch* as_batch(dtfft_gb_batch_t b) {
+    Batch* q = reinterpret_cast<Batch*>(b);
+    if (!q || q->magic != kBatchMagic) return nullptr;
+    return q;
+}
+
+static dtfft_error_t capture_batch(Batch& b, void* const* ins, void* const* outs, void* const* auxs, bool fwd) {
+    const int n = (int)b.plans.size(), K = (int)b.lanes.size();
+    GB_CUDA_TRY(cudaStreamBeginCapture(b.cap, cudaStreamCaptureModeThreadLocal));
+    dtfft_error_t e = DTFFT_SUCCESS;
+    if (cudaEventRecord(b.fork, b.cap) != cudaSuccess) e = DTFFT_ERROR_GPU_CALL_FAILED;
+    for (int l = 0; l < K && e == DTFFT_SUCCESS; ++l)
+        if (cudaStreamWaitEvent(b.lanes[l], b.fork, 0) != cudaSuccess) e = DTFFT_ERROR_GPU_CALL_FAILED;
+    for (int i = 0; i < n && e == DTFFT_SUCCESS; ++i) {
+        Plan& p = *b.plans[i];
+        cudaStream_t saved = p.stream;
+        p.stream = b.lanes[i % K];
+        e = run_execute(p, ins[i], outs[i], fwd, auxs[i], ins[i] == outs[i]);
+        p.stream = saved;
+    }
+    for (int l = 0; l < K && e == DTFFT_SUCCESS; ++l) {
+        if (cudaEventRecord(b.joins[l], b.lanes[l]) != cudaSuccess ||
+            cudaStreamWaitEvent(b.cap, b.joins[l], 0) != cudaSuccess)
+            e = DTFFT_ERROR_GPU_CALL_FAILED;
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(b.cap, &g);
+    if (e == DTFFT_SUCCESS && ce != cudaSuccess) e = DTFFT_ERROR_GPU_CALL_FAILED;
+    if (e == DTFFT_SUCCESS && cudaGraphInstantiate(&b.exec, g, 0) != cudaSuccess) e = DTFFT_ERROR_GPU_CALL_FAILED;
+    if (e != DTFFT_SUCCESS) {
+        if (g) cudaGraphDestroy(g);
+        b.exec = nullptr;
+        cudaGetLastError();
+        return e;
+    }
+    b.graph = g;
+    cudaGraphGetNodes(g, nullptr, &b.nodes);
+    return DTFFT_SUCCESS;
+}
+
+}  // namespace gb
+
+extern "C" {
+
+dtfft_error_t dtfft_gb_batch_create(int32_t n, const dtfft_plan_t* plans, int32_t lanes, dtfft_gb_batch_t* batch) {
+    if (!plans || !batch || n < 1) return DTFFT_ERROR_INVALID_USAGE;
+    *batch = nullptr;
+    Batch* b = new Batch();
+    for (int i = 0; i < n; ++i) {
+        Plan* p = as_plan(plans[i]);
+        if (!p) { delete b; return DTFFT_ERROR_PLAN_NOT_CREATED; }
+        b->plans.push_back(p);
+    }
+    const int K = std::max(1, std::min<int>(lanes > 0 ? lanes : 8, n));
+    bool ok = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int l = 0; l < K && ok; ++l) {
+        cudaStream_t s = nullptr;
+        cudaEvent_t e = nullptr;
+        ok = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+        if (s) b->lanes.push_back(s);
+        if (e) b->joins.push_back(e);
+    }
+    if (!ok) { cudaGetLastError(); delete b; return DTFFT_ERROR_GPU_CALL_FAILED; }
+    *batch = reinterpret_cast<dtfft_gb_batch_t>(b);
+    return DTFFT_SUCCESS;
+}
+
+dtfft_error_t dtfft_gb_batch_execute(dtfft_gb_batch_t batch, void* const* ins, void* const* outs, void* const* auxs,
+                                     dtfft_execute_t execute_type, void* stream) {
+    Batch* b = as_batch(batch);
+    if (!b) return DTFFT_ERROR_INVALID_USAGE;
+    if (!ins || !outs) return DTFFT_ERROR_INVALID_USAGE;
+    const int n = (int)b->plans.size();
+    std::vector<const void*> key;
+    key.reserve(3 * n + 1);
+    key.push_back((const void*)(intptr_t)execute_type);
+    for (int i = 0; i < n; ++i) {
+        key.push_back(ins[i]);
+        key.push_back(outs[i]);
+        key.push_back(auxs ? auxs[i] : nullptr);
+    }
+    if (!b->exec || key != b->key) {
+        // new buffers: check them like dtfft_execute, make the plans' aux
+        // buffers now (outside the capture) and capture the schedules again
+        b->drop_graph();
+        std::vector<void*> a(n);
+        for (int i = 0; i < n; ++i) {
+            void* ua = auxs ? auxs[i] : nullptr;
+            GB_TRY(execute_checks(b->plans[i], ins[i], outs[i], (int)execute_type, ua));
+            GB_TRY(get_aux(*b->plans[i], ua, &a[i]));
+        }
+        GB_TRY(capture_batch(*b, ins, outs, a.data(), execute_type == DTFFT_EXECUTE_FORWARD));
+        b->key = key;
+    }
+    GB_CUDA_TRY(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+    return DTFFT_SUCCESS;
+}
+
+dtfft_error_t dtfft_gb_batch_graph_nodes(dtfft_gb_batch_t batch, int64_t* nodes) {
+    Batch* b = as_batch(batch);
+    if (!b || !nodes) return DTFFT_ERROR_INVALID_USAGE;
+    *nodes = (int64_t)b->nodes;
+    return DTFFT_SUCCESS;
+}
+
+dtfft_error_t dtfft_gb_batch_destroy(dtfft_gb_batch_t* batch) {
+    if (!batch) return DTFFT_ERROR_INVALID_USAGE;
+    Batch* b = as_batch(*batch);
+    if (!b) return DTFFT_ERROR_INVALID_USAGE;
+    cudaDeviceSynchronize();
+    delete b;
+    *batch = nullptr;
+    return DTFFT_SUCCESS;
 }
 
 }  // extern "C"

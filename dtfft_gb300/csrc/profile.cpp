@@ -38,6 +38,12 @@ bool profiling() { return g_prof_on; }
 
 void* prof_begin(cudaStream_t s) {
     if (!g_prof_on) return nullptr;
+    // launches captured into a graph are not timed (their events never complete as recorded here)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return nullptr;
+    }
     std::lock_guard<std::mutex> lk(g_pmu);
     Pending* p = new Pending();
     p->a = take_event();

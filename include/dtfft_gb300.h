@@ -160,6 +160,39 @@ dtfft_error_t dtfft_execute_noalloc(dtfft_plan_t plan, void* in, void* out, dtff
 /** Size in bytes of the fixed scratch buffer of dtfft_execute_noalloc. */
 size_t dtfft_execute_noalloc_max_bytes(void);
 
+/* ------------------------------------------------------------------------ */
+/* Batches of independent plans (no counterpart in the reference, whose      */
+/* callers run one dtfft_execute per plan).                                  */
+/* ------------------------------------------------------------------------ */
+typedef struct gb_batch_s* dtfft_gb_batch_t;
+
+/**
+ * Groups `n` existing plans (any kinds, shapes, precisions and grids) so that
+ * dtfft_gb_batch_execute runs all of them with one CUDA graph launch.  The
+ * plans stay owned by the caller and must outlive the batch.  `lanes` (<= 0:
+ * 8) is the number of graph branches the plans are spread over, so the
+ * kernels of small transforms run side by side.
+ */
+dtfft_error_t dtfft_gb_batch_create(int32_t n, const dtfft_plan_t* plans, int32_t lanes, dtfft_gb_batch_t* batch);
+
+/**
+ * Same results as dtfft_execute(plans[i], ins[i], outs[i], execute_type,
+ * auxs ? auxs[i] : NULL) for every i, launched as one graph on `stream`
+ * (NULL: the legacy default stream).  The first call with a given set of
+ * buffers checks them, allocates the plans' aux buffers where `auxs` gives
+ * none and captures the graph (no other work may be captured on this thread
+ * meanwhile); later calls with the same buffers and direction only launch it.
+ * Calls with other buffers capture again.
+ */
+dtfft_error_t dtfft_gb_batch_execute(dtfft_gb_batch_t batch, void* const* ins, void* const* outs, void* const* auxs,
+                                     dtfft_execute_t execute_type, void* stream);
+
+/** Nodes of the batch's current graph (0 before the first execute). */
+dtfft_error_t dtfft_gb_batch_graph_nodes(dtfft_gb_batch_t batch, int64_t* nodes);
+
+/** Waits for the device, destroys the graph and the batch; the plans stay. */
+dtfft_error_t dtfft_gb_batch_destroy(dtfft_gb_batch_t* batch);
+
 /** Number of launches of this library's kernels since load (for benchmarks). */
 int64_t dtfft_gb_kernel_launch_count(void);
 
