@@ -156,6 +156,116 @@ def run_reference(args):
     return 0
 
 
+def seven_smooth(lo, hi):
+    out = []
+    for n in range(lo, hi + 1):
+        m = n
+        for q in (2, 3, 5, 7):
+            while m % q == 0:
+                m //= q
+        if m == 1:
+            out.append(n)
+    return out
+
+
+def batch_shapes(count=64, seed=5):
+    """64 independent 3D transforms: edges drawn (PCG64, seed 5) from the
+    7-smooth sizes in 48..384, alternating C2C complex64 / R2C float32."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    edges = seven_smooth(48, 384)
+    return [("c2c" if i % 2 == 0 else "r2c", [int(rng.choice(edges)) for _ in range(3)]) for i in range(count)]
+
+
+def batched_section(args, dt, dev, stream, peak):
+    """64 mixed transforms, fwd+bwd each: 64 sequential plain plans (default
+    effort, one dtfft_execute per plan and direction) against the same
+    transforms as tuned plans (EXHAUSTIVE: measured transpose tiles) replayed
+    as one CUDA graph per direction (dtfft_gb_batch_execute)."""
+    import torch
+    shapes = batch_shapes()
+    cfg = dt.Config(stream=stream.cuda_stream)
+    plain, tuned, bufs = [], [], []
+    pass_bytes = 0
+    for i, (kind, dims) in enumerate(shapes):
+        mk = dt.PlanC2C if kind == "c2c" else dt.PlanR2C
+        plain.append(mk(dims, precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT, config=cfg))
+        tuned.append(mk(dims, precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT,
+                        effort=dt.Effort.EXHAUSTIVE, config=cfg))
+        n = plain[-1].alloc_size
+        g = torch.Generator(device=dev)
+        g.manual_seed(1000 + i)
+        if kind == "c2c":
+            x = torch.complex(torch.randn(n, device=dev, generator=g), torch.randn(n, device=dev, generator=g))
+            o = torch.empty_like(x)
+            cbytes = n * 8
+        else:
+            x = torch.randn(n, device=dev, generator=g)
+            o = torch.empty(n // 2, dtype=torch.complex64, device=dev)
+            cbytes = (n // 2) * 8
+        aux = torch.empty(max(n * x.element_size(), 16) // 4, dtype=torch.float32, device=dev)
+        bufs.append((x, o, aux))
+        # unfused passes per direction: Z-slab 2D FFT (2) + X->Z + FFT Z, generic 3 FFT + 2 transposes
+        passes = 4 if plain[-1].z_slab_enabled else 5
+        pass_bytes += 2 * passes * 2 * cbytes
+    dt.set_config(dt.Config())
+    torch.cuda.synchronize()
+    ins = [b[0] for b in bufs]
+    outs = [b[1] for b in bufs]
+    auxs = [b[2] for b in bufs]
+
+    def seq_step():
+        for p, (x, o, a) in zip(plain, bufs):
+            p.execute(x, o, dt.Execute.FORWARD, a)
+        for p, (x, o, a) in zip(plain, bufs):
+            p.execute(o, x, dt.Execute.BACKWARD, a)
+
+    batch = dt.Batch(tuned, lanes=8)
+
+    def batch_step():
+        batch.execute(ins, outs, dt.Execute.FORWARD, auxs, stream)
+        batch.execute(outs, ins, dt.Execute.BACKWARD, auxs, stream)
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        k = max(3, min(args.steps, 10))
+        l0 = dt.kernel_launches()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k, (dt.kernel_launches() - l0) / k
+
+    seq_ms, seq_launch = timed(seq_step)
+    fwd_nodes = bwd_nodes = 0
+    batch_ms, _ = timed(batch_step)
+    batch.execute(ins, outs, dt.Execute.FORWARD, auxs, stream)
+    fwd_nodes = batch.graph_nodes
+    batch.execute(outs, ins, dt.Execute.BACKWARD, auxs, stream)
+    bwd_nodes = batch.graph_nodes
+    torch.cuda.synchronize()
+    batch.destroy()
+    for p in plain + tuned:
+        p.destroy()
+    n_c2c = sum(1 for k, _ in shapes if k == "c2c")
+    return {"workload": "64 3D transforms, edges 7-smooth in 48..384 (PCG64 seed 5), 32 C2C c64 + 32 R2C f32, "
+                        "N(0,1), fwd+bwd each, one process per transform",
+            "transforms": len(shapes), "c2c": n_c2c, "r2c": len(shapes) - n_c2c,
+            "sequential_plain": {"cycles_per_s": 1000.0 / seq_ms, "ms_per_cycle": seq_ms,
+                                 "kernel_launches_per_cycle": seq_launch},
+            "batched_graph": {"cycles_per_s": 1000.0 / batch_ms, "ms_per_cycle": batch_ms,
+                              "graph_launches_per_cycle": 2, "graph_nodes_per_cycle": fwd_nodes + bwd_nodes},
+            "speedup": seq_ms / batch_ms,
+            "unfused_pass_bytes_per_cycle": pass_bytes,
+            "effective_tbs": {"sequential_plain": pass_bytes / (seq_ms * 1e-3) / 1e12,
+                              "batched_graph": pass_bytes / (batch_ms * 1e-3) / 1e12}}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -307,6 +417,10 @@ def run_ours(args):
                  "effective_tbs": 4 * algo_bytes / (t_ms * 1e-3) / 1e12}
         tplan.destroy()
 
+    batched = None
+    if not args.no_batch:
+        batched = batched_section(args, dt, dev, stream, peak)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -336,6 +450,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "clocks": clk,
             "transpose_only": tonly,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     plan.destroy()
@@ -354,6 +469,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-transpose-only", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-transform batched section")
     ap.add_argument("--dims", type=int, nargs=3, default=None,
                     help="smaller C2C case for profiling (default: the 512^3 headline workload)")
     ap.add_argument("--grid", type=int, nargs=2, default=[2, 4])

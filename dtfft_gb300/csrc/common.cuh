@@ -3,6 +3,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <cstdio>
 #include <stdint.h>
 
 #include <atomic>
@@ -27,10 +29,20 @@ void* prof_begin(cudaStream_t s);
 void prof_end(void* token, const std::string& name, cudaStream_t s);
 bool profiling();
 
+// A failed CUDA call is reported on stderr (which call, where, CUDA's error
+// name) and turns into DTFFT_ERROR_GPU_CALL_FAILED.
+inline void report_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+    fprintf(stderr, "dtFFT-gb300: %s failed: %s (%s) at %s:%d\n", what, cudaGetErrorName(e), cudaGetErrorString(e),
+            file, line);
+}
+
 #define GB_CUDA_TRY(expr)                                             \
     do {                                                              \
         cudaError_t e_ = (expr);                                      \
-        if (e_ != cudaSuccess) return DTFFT_ERROR_GPU_CALL_FAILED;    \
+        if (e_ != cudaSuccess) {                                      \
+            ::gb::report_cuda_error(e_, #expr, __FILE__, __LINE__);   \
+            return DTFFT_ERROR_GPU_CALL_FAILED;                       \
+        }                                                             \
     } while (0)
 
 #define GB_TRY(expr)                                                  \

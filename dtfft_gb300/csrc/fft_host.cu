@@ -4,6 +4,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <map>
+#include <mutex>
 #include <sstream>
 
 #include "fft_kernels.cuh"
@@ -183,12 +185,26 @@ static int pipe_occupancy(int dbl, int m, int E, bool fused, int threads, size_t
 
 // Kernel attributes are set when a plan is built, never on the launch path:
 // execute then only enqueues kernels (and can be captured into a CUDA graph).
+// A kernel's dynamic shared memory limit is shared by every plan that uses the
+// kernel, so it only ever grows: a later plan with a smaller need must not
+// lower the limit an earlier plan launches with.
+static std::mutex g_attr_mu;
+static std::map<const void*, size_t> g_attr_smem;
+
 static dtfft_error_t set_smem_attrs(const void* fn, size_t smem) {
     if (!fn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-    if (smem > 48 * 1024) GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    // favour shared memory over L1 so several CTAs fit per SM
-    GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                     (int)cudaSharedmemCarveoutMaxShared));
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    auto it = g_attr_smem.find(fn);
+    if (it == g_attr_smem.end()) {
+        // favour shared memory over L1 so several CTAs fit per SM
+        GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared));
+        it = g_attr_smem.emplace(fn, 48 * 1024).first;
+    }
+    if (smem > it->second) {
+        GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        it->second = smem;
+    }
     return DTFFT_SUCCESS;
 }
 
@@ -283,8 +299,7 @@ static int pipe_occupancy(int dbl, int m, int E, bool fused, int threads, size_t
     int n = 0;
     auto one = [&](auto fn) {
         if (!fn) return;
-        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
-        cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+        if (set_smem_attrs((const void*)fn, smem) != DTFFT_SUCCESS) return;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess) n = 0;
     };
     if (dbl) { if (fused) one(pipe_fn<double, true>(m, E)); else one(pipe_fn<double, false>(m, E)); }

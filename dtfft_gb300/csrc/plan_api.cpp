@@ -972,25 +972,34 @@ namespace gb {
 
 static const uint32_t kBatchMagic = 0x47424254u;   // "GBBT"
 
+// One captured schedule: the graph of every plan's execute for one set of
+// buffers and one direction.
+struct BatchGraph {
+    std::vector<const void*> key;   // type, then in/out/aux of every plan
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    size_t nodes = 0;
+    uint64_t used = 0;
+    void drop() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr; graph = nullptr; nodes = 0;
+    }
+};
+
 struct Batch {
+    static const int kMaxGraphs = 4;   // e.g. forward and backward over two buffer sets
     uint32_t magic = kBatchMagic;
     std::vector<Plan*> plans;
     std::vector<cudaStream_t> lanes;
     cudaStream_t cap = nullptr;
     cudaEvent_t fork = nullptr;
     std::vector<cudaEvent_t> joins;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    std::vector<const void*> key;   // type, then in/out/aux of every plan
-    size_t nodes = 0;
-    void drop_graph() {
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        exec = nullptr; graph = nullptr; nodes = 0;
-        key.clear();
-    }
+    std::vector<BatchGraph> graphs;
+    uint64_t tick = 0;
+    size_t last_nodes = 0;
     ~Batch() {
-        drop_graph();
+        for (auto& g : graphs) g.drop();
         for (auto l : lanes) cudaStreamDestroy(l);
         for (auto e : joins) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
@@ -1005,7 +1014,8 @@ static Batch* as_batch(dtfft_gb_batch_t b) {
     return q;
 }
 
-static dtfft_error_t capture_batch(Batch& b, void* const* ins, void* const* outs, void* const* auxs, bool fwd) {
+static dtfft_error_t capture_batch(Batch& b, BatchGraph& bg, void* const* ins, void* const* outs, void* const* auxs,
+                                   bool fwd) {
     const int n = (int)b.plans.size(), K = (int)b.lanes.size();
     GB_CUDA_TRY(cudaStreamBeginCapture(b.cap, cudaStreamCaptureModeThreadLocal));
     dtfft_error_t e = DTFFT_SUCCESS;
@@ -1027,15 +1037,15 @@ static dtfft_error_t capture_batch(Batch& b, void* const* ins, void* const* outs
     cudaGraph_t g = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(b.cap, &g);
     if (e == DTFFT_SUCCESS && ce != cudaSuccess) e = DTFFT_ERROR_GPU_CALL_FAILED;
-    if (e == DTFFT_SUCCESS && cudaGraphInstantiate(&b.exec, g, 0) != cudaSuccess) e = DTFFT_ERROR_GPU_CALL_FAILED;
+    if (e == DTFFT_SUCCESS && cudaGraphInstantiate(&bg.exec, g, 0) != cudaSuccess) e = DTFFT_ERROR_GPU_CALL_FAILED;
     if (e != DTFFT_SUCCESS) {
         if (g) cudaGraphDestroy(g);
-        b.exec = nullptr;
+        bg.exec = nullptr;
         cudaGetLastError();
         return e;
     }
-    b.graph = g;
-    cudaGraphGetNodes(g, nullptr, &b.nodes);
+    bg.graph = g;
+    cudaGraphGetNodes(g, nullptr, &bg.nodes);
     return DTFFT_SUCCESS;
 }
 
@@ -1082,27 +1092,41 @@ dtfft_error_t dtfft_gb_batch_execute(dtfft_gb_batch_t batch, void* const* ins, v
         key.push_back(outs[i]);
         key.push_back(auxs ? auxs[i] : nullptr);
     }
-    if (!b->exec || key != b->key) {
+    BatchGraph* hit = nullptr;
+    for (auto& g : b->graphs) if (g.exec && g.key == key) hit = &g;
+    if (!hit) {
         // new buffers: check them like dtfft_execute, make the plans' aux
-        // buffers now (outside the capture) and capture the schedules again
-        b->drop_graph();
+        // buffers now (outside the capture) and capture the schedules; the
+        // least recently used graph makes room
         std::vector<void*> a(n);
         for (int i = 0; i < n; ++i) {
             void* ua = auxs ? auxs[i] : nullptr;
             GB_TRY(execute_checks(b->plans[i], ins[i], outs[i], (int)execute_type, ua));
             GB_TRY(get_aux(*b->plans[i], ua, &a[i]));
         }
-        GB_TRY(capture_batch(*b, ins, outs, a.data(), execute_type == DTFFT_EXECUTE_FORWARD));
-        b->key = key;
+        if ((int)b->graphs.size() >= Batch::kMaxGraphs) {
+            auto lru = std::min_element(b->graphs.begin(), b->graphs.end(),
+                                        [](const BatchGraph& x, const BatchGraph& y) { return x.used < y.used; });
+            cudaStreamSynchronize((cudaStream_t)stream);
+            lru->drop();
+            b->graphs.erase(lru);
+        }
+        BatchGraph bg;
+        GB_TRY(capture_batch(*b, bg, ins, outs, a.data(), execute_type == DTFFT_EXECUTE_FORWARD));
+        bg.key = key;
+        b->graphs.push_back(bg);
+        hit = &b->graphs.back();
     }
-    GB_CUDA_TRY(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+    hit->used = ++b->tick;
+    b->last_nodes = hit->nodes;
+    GB_CUDA_TRY(cudaGraphLaunch(hit->exec, (cudaStream_t)stream));
     return DTFFT_SUCCESS;
 }
 
 dtfft_error_t dtfft_gb_batch_graph_nodes(dtfft_gb_batch_t batch, int64_t* nodes) {
     Batch* b = as_batch(batch);
     if (!b || !nodes) return DTFFT_ERROR_INVALID_USAGE;
-    *nodes = (int64_t)b->nodes;
+    *nodes = (int64_t)b->last_nodes;
     return DTFFT_SUCCESS;
 }
 

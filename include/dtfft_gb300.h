@@ -182,12 +182,13 @@ dtfft_error_t dtfft_gb_batch_create(int32_t n, const dtfft_plan_t* plans, int32_
  * buffers checks them, allocates the plans' aux buffers where `auxs` gives
  * none and captures the graph (no other work may be captured on this thread
  * meanwhile); later calls with the same buffers and direction only launch it.
- * Calls with other buffers capture again.
+ * The batch keeps the graphs of its 4 most recently used buffer sets and
+ * directions; other calls capture again.
  */
 dtfft_error_t dtfft_gb_batch_execute(dtfft_gb_batch_t batch, void* const* ins, void* const* outs, void* const* auxs,
                                      dtfft_execute_t execute_type, void* stream);
 
-/** Nodes of the batch's current graph (0 before the first execute). */
+/** Nodes of the graph the last dtfft_gb_batch_execute launched (0 before the first). */
 dtfft_error_t dtfft_gb_batch_graph_nodes(dtfft_gb_batch_t batch, int64_t* nodes);
 
 /** Waits for the device, destroys the graph and the batch; the plans stay. */

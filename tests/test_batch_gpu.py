@@ -97,3 +97,25 @@ def test_batch_replay_follows_contents(dt, cuda):
     assert not np.array_equal(outs[0], outs[1])
     batch.destroy()
     p.destroy()
+
+
+def test_plans_sharing_a_kernel_keep_their_smem_limits(dt, cuda):
+    """Two plans whose column FFTs use the same kernel with different shared
+    memory: the second plan's creation must not lower the first one's limit."""
+    import torch
+    big = dt.PlanC2C([48, 384, 64], precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT)
+    small = dt.PlanC2C([48, 98, 64], precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT)
+    for p, dims in ((big, [48, 384, 64]), (small, [48, 98, 64]), (big, [48, 384, 64])):
+        n = p.alloc_size
+        x = random_global((n,), np.complex64, seed=n)
+        a = torch.from_numpy(x).to(cuda)
+        b = torch.zeros_like(a)
+        torch.cuda.synchronize()
+        p.execute(a, b, dt.Execute.FORWARD)
+        torch.cuda.synchronize()
+        g = x[: int(np.prod(dims))].astype(np.complex128).reshape(dims[::-1])
+        ref = np.fft.fftn(g).transpose(1, 2, 0).ravel()
+        got = b.cpu().numpy()[: ref.size]
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 1e-5
+    big.destroy()
+    small.destroy()
