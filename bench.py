@@ -242,6 +242,20 @@ def batched_section(args, dt, dev, stream, peak):
         return e0.elapsed_time(e1) / k, (dt.kernel_launches() - l0) / k
 
     seq_ms, seq_launch = timed(seq_step)
+    # where the sequential cycle's time goes, per kernel class (live event timing)
+    L = dt.lib()
+    L.dtfft_gb_profile_start()
+    seq_step()
+    torch.cuda.synchronize()
+    L.dtfft_gb_profile_stop()
+    classes = {}
+    for name, cnt, tms in _profile_results(L):
+        cls = name.split("_m")[0] if "_m" in name else name
+        c = classes.setdefault(cls, [0, 0.0])
+        c[0] += cnt
+        c[1] += tms
+    kernel_classes = [{"class": k, "launches": v[0], "total_ms": v[1]}
+                      for k, v in sorted(classes.items(), key=lambda kv: -kv[1][1])]
     fwd_nodes = bwd_nodes = 0
     batch_ms, _ = timed(batch_step)
     batch.execute(ins, outs, dt.Execute.FORWARD, auxs, stream)
@@ -261,9 +275,96 @@ def batched_section(args, dt, dev, stream, peak):
             "batched_graph": {"cycles_per_s": 1000.0 / batch_ms, "ms_per_cycle": batch_ms,
                               "graph_launches_per_cycle": 2, "graph_nodes_per_cycle": fwd_nodes + bwd_nodes},
             "speedup": seq_ms / batch_ms,
+            "sequential_kernel_classes": kernel_classes,
             "unfused_pass_bytes_per_cycle": pass_bytes,
             "effective_tbs": {"sequential_plain": pass_bytes / (seq_ms * 1e-3) / 1e12,
                               "batched_graph": pass_bytes / (batch_ms * 1e-3) / 1e12}}
+
+
+def tensor_core_section(args, dt, dev, stream, sizes=(768, 1024)):
+    """C2C complex64 N^3 (one process, Z-slab plan), inputs uniform[-1,1) re/im
+    plus 1e3-amplitude spikes at 0.1% of the points: FP32 Stockham row passes
+    against the tensor-core form (DFT-matrix GEMMs on tcgen05, FP16 hi + lo,
+    FP32 accumulate), fwd+bwd cycles/s and forward error against an FP64
+    (complex128) plan of the same transform."""
+    import torch
+    L = dt.lib()
+    L.dtfft_gb_set_fft_form.argtypes = [ctypes.c_int32]
+    out = []
+    for N in sizes:
+        dims = [N, N, N]
+        cfg = dt.Config(stream=stream.cuda_stream)
+        plans = {}
+        for form in (0, 1):
+            L.dtfft_gb_set_fft_form(form)
+            plans[form] = dt.PlanC2C(dims, precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT, config=cfg)
+        L.dtfft_gb_set_fft_form(0)
+        p64 = dt.PlanC2C(dims, precision=dt.Precision.DOUBLE, executor=dt.Executor.CUFFT, config=cfg)
+        dt.set_config(dt.Config())
+        n = plans[0].alloc_size
+        g = torch.Generator(device=dev)
+        g.manual_seed(4)
+        x0 = torch.complex(torch.rand(n, device=dev, generator=g) * 2 - 1,
+                           torch.rand(n, device=dev, generator=g) * 2 - 1)
+        spikes = torch.randint(0, n, (max(1, n // 1000),), device=dev, generator=g)
+        x0[spikes] *= 1e3
+        # FP64 reference spectrum
+        a64 = x0.to(torch.complex128)
+        b64 = torch.empty_like(a64)
+        aux64 = torch.empty_like(a64)
+        torch.cuda.synchronize()
+        p64.execute(a64, b64, dt.Execute.FORWARD, aux64)
+        torch.cuda.synchronize()
+        del a64, aux64
+        ref_norm = float(torch.linalg.vector_norm(b64))
+        a = torch.empty_like(x0)
+        b = torch.empty_like(x0)
+        aux = torch.empty_like(x0)
+        row = {"dims": dims, "points": n}
+        for form, name in ((0, "fp32_stockham"), (1, "tensor_core_fp16x3")):
+            p = plans[form]
+            a.copy_(x0)
+            torch.cuda.synchronize()
+            p.execute(a, b, dt.Execute.FORWARD, aux)
+            torch.cuda.synchronize()
+            err = float(torch.linalg.vector_norm(b.to(torch.complex128) - b64)) / ref_norm
+            p.execute(b, a, dt.Execute.BACKWARD, aux)
+            torch.cuda.synchronize()
+            rt = float(torch.linalg.vector_norm(a / n - x0) / torch.linalg.vector_norm(x0))
+
+            def step():
+                p.execute(a, b, dt.Execute.FORWARD, aux)
+                p.execute(b, a, dt.Execute.BACKWARD, aux)
+
+            for _ in range(max(args.warmup, 3)):
+                a.copy_(x0)
+                step()
+            torch.cuda.synchronize()
+            k = max(3, min(args.steps, 10))
+            L.dtfft_gb_profile_start()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(k):
+                step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            L.dtfft_gb_profile_stop()
+            ms = e0.elapsed_time(e1) / k
+            prof = sorted(_profile_results(L), key=lambda r: -r[2])
+            rows = [r for r in prof if "rows_c2c" in r[0]]
+            row[name] = {"cycles_per_s": 1000.0 / ms, "ms_per_cycle": ms, "fwd_rel_l2_vs_fp64": err,
+                         "roundtrip_rel_l2": rt,
+                         "row_pass_kernel": rows[0][0] if rows else None,
+                         "row_pass_ms": rows[0][2] / max(rows[0][1], 1) if rows else None,
+                         "kernels": [{"name": r[0], "launches": r[1], "total_ms": r[2]} for r in prof]}
+        row["speedup_tc_vs_fp32"] = row["fp32_stockham"]["ms_per_cycle"] / row["tensor_core_fp16x3"]["ms_per_cycle"]
+        out.append(row)
+        for p in list(plans.values()) + [p64]:
+            p.destroy()
+        del x0, a, b, aux, b64
+        torch.cuda.empty_cache()
+    return out
 
 
 def run_ours(args):
@@ -417,6 +518,10 @@ def run_ours(args):
                  "effective_tbs": 4 * algo_bytes / (t_ms * 1e-3) / 1e12}
         tplan.destroy()
 
+    tensor_core = None
+    if not args.no_tc:
+        tensor_core = tensor_core_section(args, dt, dev, stream)
+
     batched = None
     if not args.no_batch:
         batched = batched_section(args, dt, dev, stream, peak)
@@ -451,6 +556,7 @@ def run_ours(args):
             "clocks": clk,
             "transpose_only": tonly,
             "batched": batched,
+            "tensor_core": tensor_core,
         }
         print(json.dumps(line), flush=True)
     plan.destroy()
@@ -470,6 +576,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-transpose-only", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-transform batched section")
+    ap.add_argument("--no-tc", action="store_true", help="skip the tensor-core 768^3 / 1024^3 section")
     ap.add_argument("--dims", type=int, nargs=3, default=None,
                     help="smaller C2C case for profiling (default: the 512^3 headline workload)")
     ap.add_argument("--grid", type=int, nargs=2, default=[2, 4])

@@ -41,6 +41,15 @@ bool make_schedule(int m, Schedule& s);
 
 struct FftStep;  // one kernel launch of a plan
 
+// Arithmetic form of the C2C FP32 row passes: 0 = FP32 Stockham kernels,
+// 1 = tensor-core DFT-matrix GEMM stages with FP16 hi/lo operands (fft_tc.cu)
+// for the row lengths that have one.  Read when a plan is built.
+int fft_form();
+bool tc_supported(int m);
+dtfft_error_t tc_create(int m, void** out);
+void tc_destroy(void* tc);
+dtfft_error_t tc_execute(void* tc, const void* in, void* out, i64 nsig, int sign, int* status, cudaStream_t s);
+
 class FftPlan {
 public:
     static dtfft_error_t create(const FftDesc& d, FftPlan** out);

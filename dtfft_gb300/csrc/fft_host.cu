@@ -69,7 +69,19 @@ struct FftStep {
     size_t pipe_smem = 0;
     int pipe_ctas_per_sm = 0;
     bool reads_out = false;  // step reads the plan's output buffer (second pass)
+    void* tc = nullptr;      // tensor-core form of this step (C2C FP32 rows), see fft_tc.cu
+    ~FftStep() { tc_destroy(tc); }
 };
+
+static int g_fft_form = -1;
+
+int fft_form() {
+    if (g_fft_form < 0) {
+        const char* e = getenv("DTFFT_GB_FFT_FORM");
+        g_fft_form = (e && atoi(e) == 1) ? 1 : 0;
+    }
+    return g_fft_form;
+}
 
 // Register-kernel schedule: points per thread E (compiled: 8, 16, 24, 20, 28),
 // radices dividing E, fewest stages first, then fewest registers.
@@ -191,8 +203,20 @@ static int pipe_occupancy(int dbl, int m, int E, bool fused, int threads, size_t
 static std::mutex g_attr_mu;
 static std::map<const void*, size_t> g_attr_smem;
 
+static size_t max_optin_smem() {
+    static size_t v = 0;
+    if (!v) {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || n <= 0) n = 48 * 1024;
+        v = (size_t)n;
+    }
+    return v;
+}
+
 static dtfft_error_t set_smem_attrs(const void* fn, size_t smem) {
     if (!fn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    if (smem > max_optin_smem()) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;   // the variant cannot launch
     std::lock_guard<std::mutex> lk(g_attr_mu);
     auto it = g_attr_smem.find(fn);
     if (it == g_attr_smem.end()) {
@@ -244,6 +268,8 @@ static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
     } else if (!make_schedule(m, S.sched)) {
         return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     }
+    if (fft_form() == 1 && !S.cols && !S.dbl && S.mode == M_C2C && S.idist == m && S.odist == m && tc_supported(m))
+        GB_TRY(tc_create(m, &S.tc));
     if (S.E) goto tables;
     {
     const size_t per_sig = 2 * (size_t)m * es;   // ping-pong buffers
@@ -331,6 +357,14 @@ static dtfft_error_t launch_pipe(const PArgs<R>& P, int E, int threads, size_t s
 
 template <typename R, bool COLS>
 static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, cudaStream_t s) {
+    if (S.tc) {
+        void* tok = prof_begin(s);
+        GB_TRY(tc_execute(S.tc, in, out, S.nsig, S.sign, status_ptr(), s));
+        if (tok) prof_end(tok, std::string("ffttc_rows_c2c_m") + std::to_string(S.m) + "_f32", s);
+        count_launch();
+        GB_CUDA_TRY(cudaGetLastError());
+        return DTFFT_SUCCESS;
+    }
     Args<R> A;
     typedef typename CT<R>::T C;
     if (!COLS && S.pipe && S.pipe_ctas_per_sm > 0 && ((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
@@ -648,3 +682,11 @@ extern "C" int32_t dtfft_gb_device_status(int32_t reset) {
     }
     return v;
 }
+
+extern "C" int32_t dtfft_gb_set_fft_form(int32_t form) {
+    if (form != 0 && form != 1) return DTFFT_ERROR_INVALID_USAGE;
+    gb::g_fft_form = form;
+    return DTFFT_SUCCESS;
+}
+
+extern "C" int32_t dtfft_gb_get_fft_form(void) { return gb::fft_form(); }

@@ -1,0 +1,451 @@
+// Tensor-core form of the batched C2C FP32 row FFT (tcgen05, sm_103a).
+//
+// A row of length m = R1 * R2 is transformed in two DFT-matrix GEMM stages
+// (four-step FFT, x[n1 + R1*n2]):
+//   stage 1  Y[n1][k2] = sum_n2 x[n1 + R1*n2] * W_R2^(n2*k2)    (DFT-R2 per (row, n1))
+//   twiddle  Y[n1][k2] *= W_m^(n1*k2)                            (FP32)
+//   stage 2  X[k1*R2 + k2] = sum_n1 Y[n1][k2] * W_R1^(n1*k1)    (DFT-R1 per (row, k2))
+// Each stage is D[v][n] = sum_k A[v][k] * B[n][k]: the rows of A are 128
+// complex vectors (interleaved re/im, K = 2R), B is the real 2R x 2R form of
+// the complex DFT matrix.  Operands are split into FP16 hi + lo parts and the
+// three products hi*hi + hi*lo + lo*hi accumulate in FP32 in tensor memory
+// (lo*lo, below 2^-22 of the result, is dropped).  Every row is scaled by a
+// power of two before each split (exact) so that FP16's range holds any input
+// and the lo parts stay normal numbers.
+//
+// One CTA of 128 threads owns S = 128 / R1 rows per tile and walks tiles
+// persistently.  Thread t builds A row t of stage 1 and, after the MMA, reads
+// TMEM lane t back (tcgen05.ld), applies the twiddles and scatters stage 2's
+// A rows; one elected thread issues the tcgen05.mma instructions and commits
+// them to an mbarrier.  Every wait is bounded: on timeout the kernel records
+// an error code in the status word, waits (bounded) once more for its own MMAs
+// and frees its tensor memory before returning.
+#include <cuda_fp16.h>
+
+#include <cmath>
+#include <vector>
+
+#include "fft.cuh"
+#include "fft_kernels.cuh"
+
+namespace gb {
+
+struct TcArgs {
+    const float2* in;
+    float2* out;
+    i64 nsig;
+    i64 ntiles;
+    const uint4* bmat;    // stage-1 hi, stage-1 lo, stage-2 hi, stage-2 lo, in shared-memory byte order
+    const float2* tw;     // W_m^j, j in [0, m), for this direction
+    int* status;
+};
+
+// --- tcgen05 / shared-memory descriptors -----------------------------------
+
+// K-major operand without swizzle: 8-row x 16-byte core matrices, core
+// matrices adjacent in K are `lbo` bytes apart, adjacent in M/N `sbo` bytes.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;   // descriptor version of sm_100 and later
+    return d;                 // base offset 0, layout: no swizzle
+}
+
+// kind::f16 instruction descriptor: A, B FP16, D FP32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 lanes x 16 consecutive 32-bit columns per warp: thread i gets lane (base + i)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// byte offset of element (row, k) of a K-major no-swizzle operand with K columns
+__host__ __device__ constexpr uint32_t kmaj_off(int row, int k, int K) {
+    return (uint32_t)((row >> 3) * (K * 16) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// Operands are scaled so that the row's largest magnitude lies in
+// [2^13, 2^14): FP16 holds it (max 65504) and the lo part of every value down
+// to 2^-17 of the maximum stays a normal FP16 number (22 significant bits).
+// Returns 2^(14-e) with amax in [2^(e-1), 2^e) (e = 0 for amax = 0).
+__device__ __forceinline__ float pow2_scale(float amax, int& e) {
+    e = (int)((__float_as_uint(amax) >> 23) & 0xff) - 126;
+    if (amax == 0.f) e = 0;
+    e = max(-100, min(100, e));
+    return __uint_as_float((uint32_t)(127 + 14 - e) << 23);
+}
+
+template <int R1, int R2>
+struct TcShape {
+    static constexpr int M = R1 * R2;
+    static constexpr int S = 128 / R1;                 // rows per tile
+    static constexpr int K1 = 2 * R2, N1 = 2 * R2;     // stage 1 GEMM (real)
+    static constexpr int K2 = 2 * R1, N2 = 2 * R1;     // stage 2 GEMM (real)
+    static constexpr int G2 = (S * R2 + 127) / 128;    // stage-2 groups of 128 vectors
+    static constexpr int B1 = N1 * K1 * 2, B2 = N2 * K2 * 2;   // bytes of one fp16 B operand
+    static constexpr int A1 = 128 * K1 * 2, A2 = G2 * 128 * K2 * 2;
+    static constexpr int OFF_B1H = 0, OFF_B1L = B1, OFF_B2H = 2 * B1, OFF_B2L = 2 * B1 + B2;
+    static constexpr int OFF_A1H = 2 * (B1 + B2), OFF_A1L = OFF_A1H + A1;
+    static constexpr int OFF_A2H = OFF_A1L + A1, OFF_A2L = OFF_A2H + A2;
+    static constexpr int OFF_SCALE = OFF_A2L + A2;                 // S floats
+    static constexpr int OFF_BAR = (OFF_SCALE + 4 * S + 15) & ~15;  // mbarrier + tmem slot
+    static constexpr int SMEM = OFF_BAR + 16;
+    static constexpr int COLS_USED = N1 + G2 * N2;
+    static constexpr int TMEM_COLS = COLS_USED <= 32 ? 32 : COLS_USED <= 64 ? 64 : COLS_USED <= 128 ? 128 : 256;
+    static_assert(128 % R1 == 0, "R1 divides 128");
+    static_assert(K1 % 16 == 0 && K2 % 16 == 0, "K multiple of 16");
+    static_assert(N1 % 16 == 0 && N2 % 16 == 0 && N1 <= 256 && N2 <= 256, "N for M = 128");
+    static_assert(N1 % 16 == 0 && N2 % 16 == 0, "TMEM loads of 16 columns");
+    static_assert(COLS_USED <= 256, "tensor memory budget");
+};
+
+template <int R1, int R2>
+__global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
+    typedef TcShape<R1, R2> SH;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int t = threadIdx.x, warp = t >> 5;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + SH::OFF_BAR);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + SH::OFF_BAR + 8);
+    float* scale_inv = reinterpret_cast<float*>(sm + SH::OFF_SCALE);
+
+    // B operands (hi/lo of both stages) and zeroed stage-2 A (its padding rows stay zero)
+    {
+        const int nb = (2 * (SH::B1 + SH::B2)) / 16;
+        uint4* dst = reinterpret_cast<uint4*>(sm);
+        for (int i = t; i < nb; i += 128) dst[i] = A.bmat[i];
+        uint4 z = make_uint4(0, 0, 0, 0);
+        uint4* a2 = reinterpret_cast<uint4*>(sm + SH::OFF_A2H);
+        for (int i = t; i < (2 * SH::A2) / 16; i += 128) a2[i] = z;
+    }
+    if (t == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"((uint32_t)SH::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t sbase = smem_u32(sm);
+    const uint32_t id1 = idesc_f16(128, SH::N1), id2 = idesc_f16(128, SH::N2);
+    uint32_t phase = 0;
+    bool failed = false;
+
+    const int s1 = t / R1, n1 = t % R1;     // stage-1 row of this thread
+    for (i64 tile = blockIdx.x; tile < A.ntiles && !failed; tile += gridDim.x) {
+        const i64 sig0 = tile * SH::S;
+        // ---- stage 1 operand: row t = (s1, n1), k = 2*n2 + {re, im} ----
+        {
+            const i64 sig = sig0 + s1;
+            const bool live = sig < A.nsig;
+            float2 x[R2];
+            float amax = 0.f;
+#pragma unroll
+            for (int n2 = 0; n2 < R2; ++n2) {
+                x[n2] = live ? A.in[sig * SH::M + n1 + R1 * n2] : make_float2(0.f, 0.f);
+                amax = fmaxf(amax, fmaxf(fabsf(x[n2].x), fabsf(x[n2].y)));
+            }
+#pragma unroll
+            for (int o = 1; o < R1; o <<= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+            int e;
+            const float sc = pow2_scale(amax, e);
+            // stage-1 results are below 2 R2 2^14 in these units; stage 2 works on
+            // them times 2^-6, so its results carry the factor 2^(14-e-6)
+            if (n1 == 0) scale_inv[s1] = __uint_as_float((uint32_t)(127 + e - 8) << 23);
+#pragma unroll
+            for (int kg = 0; kg < SH::K1 / 8; ++kg) {
+                __half h[8], l[8];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float2 v = x[kg * 4 + j];
+                    const float vr = v.x * sc, vi = v.y * sc;
+                    h[2 * j] = __float2half_rn(vr);
+                    h[2 * j + 1] = __float2half_rn(vi);
+                    l[2 * j] = __float2half_rn(vr - __half2float(h[2 * j]));
+                    l[2 * j + 1] = __float2half_rn(vi - __half2float(h[2 * j + 1]));
+                }
+                const uint32_t off = kmaj_off(t, kg * 8, SH::K1);
+                *reinterpret_cast<uint4*>(sm + SH::OFF_A1H + off) = *reinterpret_cast<uint4*>(h);
+                *reinterpret_cast<uint4*>(sm + SH::OFF_A1L + off) = *reinterpret_cast<uint4*>(l);
+            }
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (t == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int j = 0; j < SH::K1 / 16; ++j) {
+                const uint32_t ka = 256u * j;   // two core matrices of K per MMA
+                const uint64_t ah = smem_desc(sbase + SH::OFF_A1H + ka, 128, SH::K1 * 16);
+                const uint64_t al = smem_desc(sbase + SH::OFF_A1L + ka, 128, SH::K1 * 16);
+                const uint64_t bh = smem_desc(sbase + SH::OFF_B1H + ka, 128, SH::K1 * 16);
+                const uint64_t bl = smem_desc(sbase + SH::OFF_B1L + ka, 128, SH::K1 * 16);
+                tc_mma(tmem, ah, bh, id1, j > 0 ? 1u : 0u);
+                tc_mma(tmem, ah, bl, id1, 1u);
+                tc_mma(tmem, al, bh, id1, 1u);
+            }
+            tc_commit(bar);
+        }
+        // every thread leaves together when a wait times out
+        if (__syncthreads_or(!mbar_wait_bounded(bar, phase))) { failed = true; break; }
+        phase ^= 1;
+        tc_fence_after();
+        // ---- stage-1 results of row t, twiddles, stage-2 operand rows (s1, k2) ----
+        {
+            const float sc2 = 1.f / 64.f;   // |Y| < 2 R2 2^14 <= 2^20: back below 2^14
+#pragma unroll
+            for (int c0 = 0; c0 < SH::N1; c0 += 16) {
+                float acc[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, acc);
+                tmem_wait_ld();
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int k2 = c0 / 2 + j;
+                    float2 y = make_float2(acc[2 * j], acc[2 * j + 1]);
+                    const float2 w = __ldg(&A.tw[(n1 * k2) % SH::M]);
+                    const float2 z = make_float2((y.x * w.x - y.y * w.y) * sc2, (y.x * w.y + y.y * w.x) * sc2);
+                    const __half hr = __float2half_rn(z.x), hi_ = __float2half_rn(z.y);
+                    const __half lr = __float2half_rn(z.x - __half2float(hr));
+                    const __half li = __float2half_rn(z.y - __half2float(hi_));
+                    const int r2 = s1 * R2 + k2;
+                    const uint32_t off = (uint32_t)((r2 >> 7) * (128 * SH::K2 * 2)) + kmaj_off(r2 & 127, 2 * n1, SH::K2);
+                    *reinterpret_cast<__half2*>(sm + SH::OFF_A2H + off) = __halves2half2(hr, hi_);
+                    *reinterpret_cast<__half2*>(sm + SH::OFF_A2L + off) = __halves2half2(lr, li);
+                }
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int g = 0; g < SH::G2; ++g) {
+                const uint32_t dcol = tmem + (uint32_t)(SH::N1 + g * SH::N2);
+                const uint32_t ag = (uint32_t)(g * 128 * SH::K2 * 2);
+#pragma unroll
+                for (int j = 0; j < SH::K2 / 16; ++j) {
+                    const uint32_t ka = 256u * j;
+                    const uint64_t ah = smem_desc(sbase + SH::OFF_A2H + ag + ka, 128, SH::K2 * 16);
+                    const uint64_t al = smem_desc(sbase + SH::OFF_A2L + ag + ka, 128, SH::K2 * 16);
+                    const uint64_t bh = smem_desc(sbase + SH::OFF_B2H + ka, 128, SH::K2 * 16);
+                    const uint64_t bl = smem_desc(sbase + SH::OFF_B2L + ka, 128, SH::K2 * 16);
+                    tc_mma(dcol, ah, bh, id2, j > 0 ? 1u : 0u);
+                    tc_mma(dcol, ah, bl, id2, 1u);
+                    tc_mma(dcol, al, bh, id2, 1u);
+                }
+            }
+            tc_commit(bar);
+        }
+        if (__syncthreads_or(!mbar_wait_bounded(bar, phase))) { failed = true; break; }
+        phase ^= 1;
+        tc_fence_after();
+        // ---- stage-2 results: lane row r2 = (s, k2) holds X[k1*R2 + k2], k1 = 0..R1-1 ----
+#pragma unroll
+        for (int g = 0; g < SH::G2; ++g) {
+            const int r2 = g * 128 + t;
+            const int s = r2 / R2, k2 = r2 % R2;
+            const i64 sig = sig0 + s;
+            const bool live = s < SH::S && sig < A.nsig;
+            const float un = live ? scale_inv[s] : 0.f;
+#pragma unroll
+            for (int c0 = 0; c0 < SH::N2; c0 += 16) {
+                float acc[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(SH::N1 + g * SH::N2 + c0), acc);
+                tmem_wait_ld();
+                if (live) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int k1 = c0 / 2 + j;
+                        A.out[sig * SH::M + k1 * R2 + k2] = make_float2(acc[2 * j] * un, acc[2 * j + 1] * un);
+                    }
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();   // TMEM and A operands are rewritten by the next tile
+        tc_fence_after();
+    }
+    if (failed) {
+        if (t == 0) atomicExch(A.status, 2);
+        mbar_wait_bounded(bar, phase);   // let the committed MMAs finish before the memory goes away
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)SH::TMEM_COLS)
+                     : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+struct TcKernel { int R1, R2; const void* fn; int smem; };
+
+template <int R1, int R2>
+static TcKernel tc_entry() {
+    return TcKernel{R1, R2, (const void*)fft_tc_kernel<R1, R2>, TcShape<R1, R2>::SMEM};
+}
+
+// row lengths with a tensor-core form: m = R1 * R2
+static bool tc_pick(int m, TcKernel& k) {
+    switch (m) {
+    case 256: k = tc_entry<16, 16>(); return true;
+    case 512: k = tc_entry<16, 32>(); return true;
+    case 768: k = tc_entry<32, 24>(); return true;
+    case 1024: k = tc_entry<32, 32>(); return true;
+    default: return false;
+    }
+}
+
+bool tc_supported(int m) { TcKernel k; return tc_pick(m, k); }
+
+// B operand of a DFT-R stage: real 2R x 2R form of W_R^(j*q) (row n = output
+// component, column k = input component), split into FP16 hi and lo, laid
+// out K-major without swizzle like the kernel's shared memory.
+static void dft_operand(int R, int sign, std::vector<uint16_t>& hi, std::vector<uint16_t>& lo) {
+    const int K = 2 * R, N = 2 * R;
+    hi.assign((size_t)N * K, 0);
+    lo.assign((size_t)N * K, 0);
+    for (int j = 0; j < R; ++j)
+        for (int q = 0; q < R; ++q) {
+            const long long e = ((long long)j * q) % R;
+            const double ang = sign * 2.0 * M_PI * (double)e / (double)R;
+            const double c = std::cos(ang), s = std::sin(ang);
+            const double vals[2][2] = {{c, -s}, {s, c}};   // [out re/im][in re/im]
+            for (int a = 0; a < 2; ++a)
+                for (int b = 0; b < 2; ++b) {
+                    const int n = 2 * j + a, k = 2 * q + b;
+                    const float v = (float)vals[a][b];
+                    const __half h = __float2half_rn(v);
+                    const __half l = __float2half_rn(v - __half2float(h));
+                    const uint32_t off = kmaj_off(n, k, K) / 2;
+                    hi[off] = __half_as_ushort(h);
+                    lo[off] = __half_as_ushort(l);
+                }
+        }
+}
+
+struct TcFft {
+    int m = 0;
+    TcKernel k{};
+    void* bmat[2] = {nullptr, nullptr};   // forward, backward
+    void* tw[2] = {nullptr, nullptr};
+    int per_sm = 0;
+    int sms = 1;
+};
+
+dtfft_error_t tc_create(int m, void** out) {
+    *out = nullptr;
+    TcKernel k;
+    if (!tc_pick(m, k)) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    TcFft* f = new TcFft();
+    f->m = m;
+    f->k = k;
+    dtfft_error_t e = DTFFT_SUCCESS;
+    for (int d = 0; d < 2 && e == DTFFT_SUCCESS; ++d) {
+        const int sign = d == 0 ? FFT_FWD : FFT_BWD;
+        std::vector<uint16_t> h1, l1, h2, l2;
+        dft_operand(k.R2, sign, h1, l1);   // stage 1: DFT-R2
+        dft_operand(k.R1, sign, h2, l2);   // stage 2: DFT-R1
+        std::vector<uint16_t> all;
+        all.insert(all.end(), h1.begin(), h1.end());
+        all.insert(all.end(), l1.begin(), l1.end());
+        all.insert(all.end(), h2.begin(), h2.end());
+        all.insert(all.end(), l2.begin(), l2.end());
+        std::vector<float> tw(2 * (size_t)m);
+        for (int j = 0; j < m; ++j) {
+            const double ang = sign * 2.0 * M_PI * (double)j / (double)m;
+            tw[2 * j] = (float)std::cos(ang);
+            tw[2 * j + 1] = (float)std::sin(ang);
+        }
+        if (cudaMalloc(&f->bmat[d], all.size() * 2) != cudaSuccess ||
+            cudaMemcpy(f->bmat[d], all.data(), all.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMalloc(&f->tw[d], tw.size() * 4) != cudaSuccess ||
+            cudaMemcpy(f->tw[d], tw.data(), tw.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+            e = DTFFT_ERROR_GPU_CALL_FAILED;
+    }
+    if (e == DTFFT_SUCCESS) {
+        if (cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, k.smem) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f->per_sm, k.fn, 128, k.smem) != cudaSuccess ||
+            f->per_sm < 1)
+            e = DTFFT_ERROR_GPU_CALL_FAILED;
+        // each CTA holds up to 256 tensor-memory columns of the SM's 512
+        f->per_sm = std::min(f->per_sm, 2);
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&f->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || f->sms < 1)
+            e = DTFFT_ERROR_GPU_CALL_FAILED;
+    }
+    if (e != DTFFT_SUCCESS) { cudaGetLastError(); tc_destroy(f); return e; }
+    *out = f;
+    return DTFFT_SUCCESS;
+}
+
+void tc_destroy(void* p) {
+    TcFft* f = static_cast<TcFft*>(p);
+    if (!f) return;
+    for (int d = 0; d < 2; ++d) {
+        if (f->bmat[d]) cudaFree(f->bmat[d]);
+        if (f->tw[d]) cudaFree(f->tw[d]);
+    }
+    delete f;
+}
+
+dtfft_error_t tc_execute(void* p, const void* in, void* out, i64 nsig, int sign, int* status, cudaStream_t s) {
+    TcFft* f = static_cast<TcFft*>(p);
+    if (nsig <= 0) return DTFFT_SUCCESS;
+    const int S = 128 / f->k.R1;
+    TcArgs A;
+    A.in = (const float2*)in;
+    A.out = (float2*)out;
+    A.nsig = nsig;
+    A.ntiles = (nsig + S - 1) / S;
+    const int d = sign == FFT_FWD ? 0 : 1;
+    A.bmat = (const uint4*)f->bmat[d];
+    A.tw = (const float2*)f->tw[d];
+    A.status = status;
+    const i64 grid = std::min<i64>(A.ntiles, (i64)f->sms * f->per_sm);
+    void* args[] = {&A};
+    GB_CUDA_TRY(cudaLaunchKernel(f->k.fn, dim3((unsigned)grid), dim3(128), args, (size_t)f->k.smem, s));
+    return DTFFT_SUCCESS;
+}
+
+}  // namespace gb

@@ -194,6 +194,20 @@ dtfft_error_t dtfft_gb_batch_graph_nodes(dtfft_gb_batch_t batch, int64_t* nodes)
 /** Waits for the device, destroys the graph and the batch; the plans stay. */
 dtfft_error_t dtfft_gb_batch_destroy(dtfft_gb_batch_t* batch);
 
+/**
+ * Arithmetic form of the complex FP32 row FFT passes of plans created from now
+ * on (no counterpart in the reference, whose FFTs come from cuFFT / VkFFT):
+ *   0  FP32 Stockham kernels (default)
+ *   1  tensor-core form: the row FFT of length 256, 512, 768 or 1024 runs as
+ *      two DFT-matrix GEMM stages on tcgen05 with FP16 hi + lo operands
+ *      (three products) accumulated in FP32, FP32 twiddles between the stages;
+ *      other lengths, FP64 and real transforms keep the FP32 kernels.
+ * The environment variable DTFFT_GB_FFT_FORM gives the initial value.
+ * Returns DTFFT_ERROR_INVALID_USAGE for any other value.
+ */
+int32_t dtfft_gb_set_fft_form(int32_t form);
+int32_t dtfft_gb_get_fft_form(void);
+
 /** Number of launches of this library's kernels since load (for benchmarks). */
 int64_t dtfft_gb_kernel_launch_count(void);
 
