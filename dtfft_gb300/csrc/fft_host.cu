@@ -83,10 +83,16 @@ int fft_form() {
     return g_fft_form;
 }
 
-// Register-kernel schedule: points per thread E (compiled: 8, 16, 24, 20, 28),
+// Register-kernel schedule: points per thread E (compiled counts below),
 // radices dividing E, fewest stages first, then fewest registers.
-static bool make_reg_schedule(int m, bool cols, int& E_out, Schedule& sch, int& T_out, int max_T = 256) {
-    static const int Es[] = {8, 16, 24, 20, 28};
+// `prec`: 0 float, 1 double (the register kernels compiled for that
+// precision), -1 the counts the fused kernels are compiled for.
+static bool make_reg_schedule(int m, bool cols, int& E_out, Schedule& sch, int& T_out, int max_T = 256,
+                              int prec = -1) {
+    static const std::vector<int> Es_fused = {8, 16, 24, 20, 28};
+    static const std::vector<int> Es_f32 = {8, 16, 24, 20, 28, 7, 9, 10, 12, 14, 15, 18, 21, 25, 30, 35, 42};
+    static const std::vector<int> Es_f64 = {8, 16, 24, 20, 28, 7, 9, 10, 12, 14, 15, 18, 21, 25};
+    const std::vector<int>& Es = prec < 0 ? Es_fused : (prec == 0 ? Es_f32 : Es_f64);
     static const int rads[] = {16, 8, 7, 5, 4, 3, 2};
     int best_stages = 1 << 30, best_E = 0;
     Schedule best;
@@ -251,7 +257,7 @@ static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
     S.sign = sign;
     const size_t es = S.dbl ? 16 : 8;
     int E = 0, T = 0;
-    if (!getenv("DTFFT_GB_NO_REG_FFT") && make_reg_schedule(m, S.cols, E, S.sched, T)) {
+    if (!getenv("DTFFT_GB_NO_REG_FFT") && make_reg_schedule(m, S.cols, E, S.sched, T, 256, S.dbl)) {
         S.E = E;
         // S signals per CTA, blockDim = S*T (signals past the end are masked)
         S.per = std::max(1, 256 / T);

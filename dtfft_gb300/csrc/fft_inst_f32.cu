@@ -3,6 +3,8 @@
 
 namespace gb {
 
+void* reg_kernel_ext_f32(int E, bool cols, bool c2c);
+
 template <>
 void* KPtr<float>::reg(int E, bool cols, bool c2c) {
 #define GB_R(E_) \
@@ -13,7 +15,7 @@ void* KPtr<float>::reg(int E, bool cols, bool c2c) {
         GB_R(8) GB_R(16) GB_R(24) GB_R(20) GB_R(28)
     }
 #undef GB_R
-    return nullptr;
+    return reg_kernel_ext_f32(E, cols, c2c);
 }
 
 template <>
