@@ -73,10 +73,16 @@ private:
 class FusedFT {
 public:
     // Fails (without side effects) when the boxes do not give every source
-    // rank whole rows of the transform axis or the length has no register schedule.
-    static dtfft_error_t create(const BoxList& bl, int m, int dbl, FusedFT** out);
+    // rank whole rows of the transform axis or the length has no register
+    // schedule; with tile_only, also when the tile kernel cannot take the rows.
+    static dtfft_error_t create(const BoxList& bl, int m, int dbl, bool tile_only, FusedFT** out);
     ~FusedFT();
     dtfft_error_t execute(const void* in, void* out, int sign, cudaStream_t s);
+    // False when this pass cannot run on these buffers (the tile kernel's bulk
+    // copies need 16-byte aligned rows); the caller then runs FFT + transpose.
+    bool usable(const void* in, const void* out) const {
+        return !tile_ || (((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0);
+    }
 
 private:
     int m_ = 0, dbl_ = 0, E_ = 0, T_ = 0, S_ = 1, pitch_ = 0, ngroups_ = 0;
@@ -84,6 +90,10 @@ private:
     size_t smem_ = 0;
     size_t pipe_smem_ = 0;   // TMA-pipelined persistent variant (0 CTAs/SM = not used)
     int pipe_per_sm_ = 0;
+    // warp-per-row tile kernel (fft_tile.cuh): used when tile_ is set
+    bool tile_ = false;
+    int tile_nst_ = 0, tile_threads_ = 0, pair_ok_ = 0;
+    const void* tw_bwd_ = nullptr;
     Schedule sched_;
     const void* tw_ = nullptr;
     const void* groups_ = nullptr;

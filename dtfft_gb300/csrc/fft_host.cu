@@ -9,6 +9,7 @@
 #include <sstream>
 
 #include "fft_kernels.cuh"
+#include "fft_tile.cuh"
 
 namespace gb {
 
@@ -70,6 +71,10 @@ struct FftStep {
     int pipe_ctas_per_sm = 0;
     bool reads_out = false;  // step reads the plan's output buffer (second pass)
     void* tc = nullptr;      // tensor-core form of this step (C2C FP32 rows), see fft_tc.cu
+    bool tile = false;       // C2C rows: warp-per-row tile kernel (fft_tile.cuh)
+    int tile_S = 0, tile_nst = 0, tile_threads = 0;
+    size_t tile_smem = 0;
+    const void* tw_dir = nullptr;   // W_m^(sign*e) for this step's direction
     ~FftStep() { tc_destroy(tc); }
 };
 
@@ -198,6 +203,39 @@ static dtfft_error_t upload_table(const std::vector<double>& t, int dbl, std::ve
 
 static const size_t kSmemBudget = 96 * 1024;
 
+// Table of W_m^(sign*e), e < m, for one direction (the tile kernels take the
+// direction's own table instead of conjugating on the fly).
+static dtfft_error_t upload_dir_table(int m, int sign, int dbl, std::vector<void*>& owned, const void** out) {
+    std::vector<double> t = table_exp(m, 1, m);
+    if (sign > 0)
+        for (int j = 0; j < m; ++j) t[2 * (size_t)j + 1] = -t[2 * (size_t)j + 1];
+    return upload_table(t, dbl, owned, out);
+}
+
+static size_t max_optin_smem();
+
+// Launch shape of the warp-per-row tile kernel for rows of m points: rows per
+// tile S (one 128-byte run per point when the tile is written transposed),
+// ring depth, threads.  False when no variant is compiled for m or the ring
+// cannot hold two tiles.
+struct TileShape { int E = 0, S = 0, nst = 0, threads = 0; size_t smem = 0; };
+static bool tile_shape(int m, int dbl, bool xpose, TileShape& ts) {
+    const int E = dbl ? TilePtr<double>::points_per_thread(m) : TilePtr<float>::points_per_thread(m);
+    if (!E || getenv("DTFFT_GB_NO_TILE")) return false;
+    const size_t es = dbl ? 16 : 8;
+    const size_t cap = max_optin_smem();
+    int S = dbl ? 8 : 16;
+    while (S > 2 && 128 + 2 * (size_t)S * m * es > cap) S >>= 1;
+    const size_t tile = (size_t)S * m * es;
+    const int nst = (int)std::min<size_t>(4, (cap - 128) / tile);
+    if (nst < 2) return false;
+    ts.E = E; ts.S = S; ts.nst = nst;
+    if (xpose) ts.threads = 32 * (xpose_compute_warps(dbl != 0, E) + xpose_store_warps(dbl != 0, E));
+    else ts.threads = 32 * std::min(S, tile_threads(dbl != 0, E) / 32);
+    ts.smem = 128 + (size_t)nst * tile;
+    return true;
+}
+
 // Fill geometry, tables and launch shape of one step.
 static int pipe_occupancy(int dbl, int m, int E, bool fused, int threads, size_t smem);
 
@@ -276,6 +314,17 @@ static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
     }
     if (fft_form() == 1 && !S.cols && !S.dbl && S.mode == M_C2C && S.idist == m && S.odist == m && tc_supported(m))
         GB_TRY(tc_create(m, &S.tc));
+    if (!S.cols && S.mode == M_C2C && S.idist == m && S.odist == m) {
+        TileShape ts;
+        if (tile_shape(m, S.dbl, false, ts)) {
+            const void* fn = S.dbl ? TilePtr<double>::get(m, sign, false) : TilePtr<float>::get(m, sign, false);
+            if (fn && set_smem_attrs(fn, ts.smem) == DTFFT_SUCCESS) {
+                S.tile = true;
+                S.tile_S = ts.S; S.tile_nst = ts.nst; S.tile_threads = ts.threads; S.tile_smem = ts.smem;
+                GB_TRY(upload_dir_table(m, sign, S.dbl, owned, &S.tw_dir));
+            }
+        }
+    }
     if (S.E) goto tables;
     {
     const size_t per_sig = 2 * (size_t)m * es;   // ping-pong buffers
@@ -373,6 +422,23 @@ static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, 
     }
     Args<R> A;
     typedef typename CT<R>::T C;
+    if (!COLS && S.tile && ((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
+        TArgs<R> P;
+        P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)S.tw_dir;
+        P.nsig = S.nsig; P.groups = nullptr; P.segs = nullptr; P.ngroups = 0;
+        P.ntiles = (S.nsig + S.tile_S - 1) / S.tile_S;
+        P.S = S.tile_S; P.nst = S.tile_nst; P.pair_ok = 0; P.status = status_ptr();
+        void (*kfn)(TArgs<R>) = (void (*)(TArgs<R>))TilePtr<R>::get(S.m, S.sign, false);
+        if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+        const i64 grid = std::min<i64>(P.ntiles, (i64)sm_count());
+        if (grid <= 0) return DTFFT_SUCCESS;
+        void* tok = prof_begin(s);
+        kfn<<<(unsigned)grid, S.tile_threads, S.tile_smem, s>>>(P);
+        if (tok) prof_end(tok, std::string("ffttile_rows_c2c_m") + std::to_string(S.m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
+        count_launch();
+        GB_CUDA_TRY(cudaGetLastError());
+        return DTFFT_SUCCESS;
+    }
     if (!COLS && S.pipe && S.pipe_ctas_per_sm > 0 && ((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
         PArgs<R> P;
         P.in = (const C*)in; P.out = (C*)out;
@@ -530,17 +596,31 @@ dtfft_error_t FftPlan::execute(const void* in, void* out, int sign, cudaStream_t
 // ---------------------------------------------------------------------------
 // FusedFT: batched C2C along the source's aligned axis + the box-list transpose
 // ---------------------------------------------------------------------------
-dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, FusedFT** out) {
+dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only, FusedFT** out) {
     *out = nullptr;
     if (bl.copy || bl.host.empty()) return DTFFT_ERROR_INVALID_USAGE;
     if (bl.elem != (dbl ? 16 : 8)) return DTFFT_ERROR_INVALID_USAGE;
-    // rows per CTA: 16 when the signal fits 32 threads, else as many as 512 threads allow
+    const size_t es = dbl ? 16 : 8;
+    // bulk copies need every source row 16-byte aligned
+    bool aligned = (m * es) % 16 == 0;
+    for (const Box& x : bl.host)
+        aligned = aligned && ((x.src_off - x.a0) * (i64)es) % 16 == 0 && (x.sb * (i64)es) % 16 == 0 &&
+                  (x.sc * (i64)es) % 16 == 0;
+    // warp-per-row tile kernel when one is compiled for m, else the register kernels
+    TileShape ts;
+    const bool tile = aligned && tile_shape(m, dbl, true, ts);
+    if (tile_only && !tile) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     int E = 0, T = 0;
     Schedule sch;
-    if (!make_reg_schedule(m, false, E, sch, T, 64) && !make_reg_schedule(m, false, E, sch, T, 256))
-        return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-    int S = 1;   // rows per CTA: a power of two, at most 16 and (S*T) within the launch bound
-    while (S * 2 <= 16 && S * 2 * T <= (dbl ? 256 : 512)) S *= 2;
+    int S = 1;
+    if (tile) {
+        S = ts.S;
+    } else {
+        if (!make_reg_schedule(m, false, E, sch, T, 64) && !make_reg_schedule(m, false, E, sch, T, 256))
+            return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+        // rows per CTA: a power of two, at most 16 and (S*T) within the launch bound
+        while (S * 2 <= 16 && S * 2 * T <= (dbl ? 256 : 512)) S *= 2;
+    }
     std::vector<FGroup> groups;
     std::vector<FSeg> segs;
     i64 ctas = 0;
@@ -581,20 +661,33 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, FusedFT** out) 
     p->m_ = m; p->dbl_ = dbl; p->E_ = E; p->T_ = T; p->S_ = S; p->sched_ = sch;
     p->ngroups_ = (int)groups.size();
     p->ctas_ = ctas;
-    const size_t es = dbl ? 16 : 8;
-    const int pitch = m + m / 16;
-    p->pitch_ = pitch;
-    p->smem_ = std::max((size_t)S * pitch, (size_t)m * (S + 1)) * es;
-    // TMA-pipelined variant: every row start must be 16-byte aligned
-    bool aligned = (m * es) % 16 == 0;
-    for (const FGroup& g : groups)
-        aligned = aligned && (g.src_off * (i64)es) % 16 == 0 && (g.su * (i64)es) % 16 == 0 &&
-                  (g.sw * (i64)es) % 16 == 0;
-    if (aligned && !getenv("DTFFT_GB_NO_PIPE")) {
-        p->pipe_smem_ = 128 + 2 * (size_t)S * m * es + p->smem_;
-        p->pipe_per_sm_ = pipe_occupancy(dbl, m, E, true, S * T, p->pipe_smem_);
+    dtfft_error_t err = DTFFT_SUCCESS;
+    if (tile) {
+        p->tile_ = true;
+        p->tile_nst_ = ts.nst;
+        p->tile_threads_ = ts.threads;
+        p->smem_ = ts.smem;
+        // two rows per 16-byte store when every destination offset and stride is even
+        int pair = dbl ? 0 : 1;
+        for (const FSeg& sgm : segs) pair = pair && (sgm.dst_off % 2 == 0) && (sgm.di % 2 == 0) && (sgm.dw % 2 == 0);
+        p->pair_ok_ = pair;
+        err = upload_dir_table(m, -1, dbl, p->owned_, &p->tw_);
+        if (err == DTFFT_SUCCESS) err = upload_dir_table(m, 1, dbl, p->owned_, &p->tw_bwd_);
+        for (int sg = -1; sg <= 1 && err == DTFFT_SUCCESS; sg += 2) {
+            const void* fn = dbl ? TilePtr<double>::get(m, sg, true) : TilePtr<float>::get(m, sg, true);
+            err = set_smem_attrs(fn, ts.smem);
+        }
+    } else {
+        const int pitch = m + m / 16;
+        p->pitch_ = pitch;
+        p->smem_ = std::max((size_t)S * pitch, (size_t)m * (S + 1)) * es;
+        // TMA-pipelined variant: every row start must be 16-byte aligned
+        if (aligned && !getenv("DTFFT_GB_NO_PIPE")) {
+            p->pipe_smem_ = 128 + 2 * (size_t)S * m * es + p->smem_;
+            p->pipe_per_sm_ = pipe_occupancy(dbl, m, E, true, S * T, p->pipe_smem_);
+        }
+        err = upload_table(table_exp(m, 1, m), dbl, p->owned_, &p->tw_);
     }
-    dtfft_error_t err = upload_table(table_exp(m, 1, m), dbl, p->owned_, &p->tw_);
     if (err == DTFFT_SUCCESS) {
         void* dg = nullptr; void* ds = nullptr;
         if (cudaMalloc(&dg, sizeof(FGroup) * groups.size()) != cudaSuccess ||
@@ -611,7 +704,9 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, FusedFT** out) 
     if (err == DTFFT_SUCCESS) {
         (void)sm_count();
         (void)status_ptr();
-        err = set_smem_attrs(dbl ? (const void*)KPtr<double>::xpose(E) : (const void*)KPtr<float>::xpose(E), p->smem_);
+        if (!tile)
+            err = set_smem_attrs(dbl ? (const void*)KPtr<double>::xpose(E) : (const void*)KPtr<float>::xpose(E),
+                                 p->smem_);
     }
     if (err != DTFFT_SUCCESS) { delete p; return err; }
     *out = p;
@@ -661,8 +756,37 @@ static dtfft_error_t launch_fused_pipe(int m, int E, int T, int S, int pitch, co
     return DTFFT_SUCCESS;
 }
 
+template <typename R>
+static dtfft_error_t launch_fused_tile(int m, int S, int nst, int threads, size_t smem, int pair_ok, const void* tw,
+                                      const void* groups, const void* segs, int ngroups, i64 tiles, const void* in,
+                                      void* out, int sign, cudaStream_t s) {
+    typedef typename CT<R>::T C;
+    TArgs<R> P;
+    P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)tw;
+    P.nsig = 0; P.groups = (const FGroup*)groups; P.segs = (const FSeg*)segs; P.ngroups = ngroups;
+    P.ntiles = tiles; P.S = S; P.nst = nst; P.pair_ok = pair_ok; P.status = status_ptr();
+    void (*kfn)(TArgs<R>) = (void (*)(TArgs<R>))TilePtr<R>::get(m, sign, true);
+    if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    const i64 grid = std::min<i64>(tiles, (i64)sm_count());
+    void* tok = prof_begin(s);
+    kfn<<<(unsigned)grid, threads, smem, s>>>(P);
+    if (tok) prof_end(tok, std::string("ffttile_xpose_m") + std::to_string(m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
+    count_launch();
+    GB_CUDA_TRY(cudaGetLastError());
+    return DTFFT_SUCCESS;
+}
+
 dtfft_error_t FusedFT::execute(const void* in, void* out, int sign, cudaStream_t s) {
     if (ctas_ == 0) return DTFFT_SUCCESS;
+    if (tile_) {
+        if (((uintptr_t)in % 16) != 0 || ((uintptr_t)out % 16) != 0) return DTFFT_ERROR_INVALID_USAGE;
+        const void* tw = sign > 0 ? tw_bwd_ : tw_;
+        if (dbl_)
+            return launch_fused_tile<double>(m_, S_, tile_nst_, tile_threads_, smem_, pair_ok_, tw, groups_, segs_,
+                                             ngroups_, ctas_, in, out, sign, s);
+        return launch_fused_tile<float>(m_, S_, tile_nst_, tile_threads_, smem_, pair_ok_, tw, groups_, segs_,
+                                        ngroups_, ctas_, in, out, sign, s);
+    }
     if (pipe_per_sm_ > 0 && ((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
         if (dbl_)
             return launch_fused_pipe<double>(m_, E_, T_, S_, pitch_, sched_, tw_, groups_, segs_, ngroups_, ctas_,

@@ -1,0 +1,418 @@
+// Warp-per-row tile kernels: batched C2C rows, optionally fused with the
+// virtual-grid transpose that follows them in the execute schedule.
+//
+// A persistent CTA walks a list of tiles of S rows.  Rows of upcoming tiles
+// stream from HBM into a ring of shared-memory buffers with cp.async.bulk
+// (completion on a transaction-count mbarrier per buffer), so the loads of
+// the next tiles overlap the work on this one.  A tile whose rows are
+// contiguous in HBM lands with a single bulk copy.
+//
+// Each row of M = 32*E points belongs to one warp: lane t keeps points
+// t + 32*q (q < E) in registers, every radix stage is local to the thread,
+// and the Stockham permutation between stages goes through the row's own
+// slot of the tile buffer.  A row therefore needs only __syncwarp between
+// stages, never a CTA barrier.  The exchange addresses are XOR-swizzled,
+// i ^ ((i >> 4) & 15), which keeps the radix-16 schedules free of
+// shared-memory bank conflicts without padding the rows.
+//
+// Output:
+//  plain (fft_tile_kernel) - the last stage stores straight from registers
+//           to the output row (32 lanes on consecutive addresses);
+//  xpose (fft_tile_xpose_kernel) - warp-specialised: compute warps transform
+//           the rows of tile k and write the spectra back into the row slots
+//           while store warps write earlier tiles out transposed.  For every
+//           point i the S rows of a tile are consecutive along the
+//           destination's contiguous axis, so each point becomes one
+//           S-element run (128 B for S = 16 complex64 rows or S = 8
+//           complex128 rows) of the destination rank's block.  A read-out
+//           swizzle keeps those column reads conflict-free.  Each buffer
+//           moves loading -> computed -> free through three mbarriers, so
+//           transforms and scattered stores overlap instead of alternating.
+//
+// The xpose kernel replaces "FFT along the aligned axis, then transpose" pairs
+// of the reference's execute_generic / execute_2d schedules
+// (src/dtfft_plan.F90:877-913, 1060-1101: fft(1) then X->Y, fft(2) then Y->Z,
+// and the backward counterparts) with one HBM pass.
+//
+// Every mbarrier wait is bounded.  A warp that gives up records an error in
+// the status word and raises a CTA-wide abort flag that ends the other
+// warps' waits; the warp that issues the bulk copies waits (bounded) for its
+// copies still in flight before it returns.
+#pragma once
+
+#include "fft_kernels.cuh"
+
+namespace gb {
+
+template <typename R>
+struct TArgs {
+    typedef typename CT<R>::T C;
+    const C* in;
+    C* out;
+    const C* tw;          // W_M^(sign*e), e < M, for this launch's direction
+    i64 nsig;             // plain: rows, row r at r*M of in and out
+    const FGroup* groups; // xpose: source rank blocks
+    const FSeg* segs;     //        destination segments of each block
+    int ngroups;
+    i64 ntiles;
+    int S;                // rows per tile (power of two)
+    int nst;              // ring depth (at most 4)
+    int pair_ok;          // xpose, complex64: destinations allow 16-byte stores of two rows
+    int* status;
+};
+
+// exchange swizzle (stays inside aligned 16-point blocks; M % 16 == 0)
+__device__ __forceinline__ int xsw(int i) { return i ^ ((i >> 4) & 15); }
+
+// read-out swizzle of row r: conflict-free column reads of the write-out
+// (lgsh = log2 of the XOR step for this S)
+template <int ES>
+__device__ __forceinline__ int osw(int r, int i, int lgsh) {
+    if constexpr (ES == 8) return i ^ (((r >> 1) << lgsh) & 15);
+    else return i ^ ((r << lgsh) & 7);
+}
+
+template <typename R, int SG, int E, int M, int Ns, int RAD, int... Rest>
+__device__ __forceinline__ void tile_stages(typename CT<R>::T (&v)[E], int t, const typename CT<R>::T* __restrict__ tw,
+                                            typename CT<R>::T* row) {
+    typedef typename CT<R>::T C;
+    constexpr int T = M / E;
+    constexpr int B = E / RAD;
+    constexpr int tstep = M / (Ns * RAD);
+    constexpr bool LAST = sizeof...(Rest) == 0;
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = t + b * T;
+        const int k = (T % Ns == 0) ? (t % Ns) : (j % Ns);
+        C w[RAD];
+#pragma unroll
+        for (int r = 0; r < RAD; ++r) w[r] = v[b + r * B];
+        if constexpr (Ns > 1) {
+            const int e1 = tstep * k;
+#pragma unroll
+            for (int r = 1; r < RAD; ++r) w[r] = cmul(w[r], __ldg(&tw[e1 * r]));
+        }
+        dft_any<R, RAD>(w, SG);
+        if constexpr (LAST) {
+#pragma unroll
+            for (int r = 0; r < RAD; ++r) v[b + r * B] = w[r];
+        } else {
+            const int base = (j - k) * RAD + k;
+#pragma unroll
+            for (int r = 0; r < RAD; ++r) row[xsw(base + r * Ns)] = w[r];
+        }
+    }
+    if constexpr (!LAST) {
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < E; ++q) v[q] = row[xsw(t + T * q)];
+        __syncwarp();
+        tile_stages<R, SG, E, M, Ns * RAD, Rest...>(v, t, tw, row);
+    }
+}
+
+// Source rows of `tile`: first row, row stride, row count, group, u0, w.
+template <typename R, bool XPOSE, int M>
+__device__ __forceinline__ void tile_geom(const TArgs<R>& A, i64 tile, i64& row0, i64& rs, int& nrows, int& gi,
+                                          int& u0, int& w) {
+    if constexpr (XPOSE) {
+        int lo = 0, hi = A.ngroups - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (A.groups[mid].cta_begin <= tile) lo = mid; else hi = mid - 1;
+        }
+        const FGroup& g = A.groups[lo];
+        const int tl = (int)(tile - g.cta_begin);
+        u0 = (tl % g.tiles_u) * A.S;
+        w = tl / g.tiles_u;
+        nrows = min(A.S, g.nu - u0);
+        row0 = g.src_off + (i64)u0 * g.su + (i64)w * g.sw;
+        rs = g.su;
+        gi = lo;
+    } else {
+        row0 = tile * A.S * (i64)M;
+        nrows = (int)min((i64)A.S, A.nsig - tile * A.S);
+        rs = M;
+        gi = 0; u0 = 0; w = 0;
+    }
+}
+
+template <typename R, bool XPOSE, int M>
+__device__ __forceinline__ void tile_issue(const TArgs<R>& A, i64 tile, typename CT<R>::T* buf, uint64_t* bar) {
+    typedef typename CT<R>::T C;
+    i64 row0, rs;
+    int nrows, gi, u0, w;
+    tile_geom<R, XPOSE, M>(A, tile, row0, rs, nrows, gi, u0, w);
+    constexpr uint32_t row_bytes = (uint32_t)(M * sizeof(C));
+    mbar_expect_tx(bar, row_bytes * (uint32_t)nrows);
+    if (rs == M) {
+        bulk_load(buf, A.in + row0, row_bytes * (uint32_t)nrows, bar);
+    } else {
+        for (int r = 0; r < nrows; ++r) bulk_load(buf + r * M, A.in + row0 + (i64)r * rs, row_bytes, bar);
+    }
+}
+
+// Load one row from its slot, transform it, and leave the spectrum in
+// registers (v[q] = point lane + 32*q).
+template <typename R, int SG, int E, int... Rs>
+__device__ __forceinline__ void tile_row_fft(typename CT<R>::T (&v)[E], typename CT<R>::T* row, int lane,
+                                             const typename CT<R>::T* tw) {
+    constexpr int M = (Rs * ... * 1);
+#pragma unroll
+    for (int q = 0; q < E; ++q) v[q] = row[lane + 32 * q];
+    __syncwarp();
+    tile_stages<R, SG, E, M, 1, Rs...>(v, lane, tw, row);
+}
+
+// ---------------------------------------------------------------------------
+// Plain rows
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int tile_threads(bool dbl, int E) { return (E >= 16 || dbl) ? 256 : 512; }
+
+template <typename R, int SG, int E, int... Rs>
+__global__ void __launch_bounds__(tile_threads(sizeof(R) == 8, E), 1) fft_tile_kernel(TArgs<R> A) {
+    typedef typename CT<R>::T C;
+    constexpr int M = (Rs * ... * 1);
+    static_assert(M == E * 32, "one warp per row");
+    static_assert(M % 16 == 0, "swizzles need 16-point blocks");
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+    C* ring = reinterpret_cast<C*>(smem_raw + 128);
+    const int S = A.S, NST = A.nst;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < NST; ++b) mbar_init(&bars[b], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int j = 0; j < NST; ++j) {
+            const i64 tj = blockIdx.x + (i64)j * gridDim.x;
+            if (tj < A.ntiles) tile_issue<R, false, M>(A, tj, ring + (i64)j * S * M, &bars[j]);
+        }
+    }
+    int b = 0;
+    uint32_t par = 0;
+    for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+        const bool ok = mbar_wait_bounded(&bars[b], par);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicExch(A.status, 1);
+                int bb = b;
+                uint32_t pp = par;
+                for (int j = 0; j < NST; ++j) {
+                    const i64 tj = tile + (i64)j * gridDim.x;
+                    if (tj >= A.ntiles) break;
+                    mbar_wait_bounded(&bars[bb], pp);
+                    if (++bb == NST) { bb = 0; pp ^= 1; }
+                }
+            }
+            __syncthreads();
+            return;
+        }
+        i64 row0, rs;
+        int nrows, gi, u0, w;
+        tile_geom<R, false, M>(A, tile, row0, rs, nrows, gi, u0, w);
+        C* tb = ring + (i64)b * S * M;
+        for (int rl = warp; rl < nrows; rl += W) {
+            C v[E];
+            tile_row_fft<R, SG, E, Rs...>(v, tb + rl * M, lane, A.tw);
+            C* dst = A.out + row0 + (i64)rl * M;
+#pragma unroll
+            for (int q = 0; q < E; ++q) dst[lane + 32 * q] = v[q];
+        }
+        // buffer b is consumed: hand it back to the bulk-copy engine
+        fence_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const i64 tn = tile + (i64)NST * gridDim.x;
+            if (tn < A.ntiles) tile_issue<R, false, M>(A, tn, tb, &bars[b]);
+        }
+        if (++b == NST) { b = 0; par ^= 1; }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Rows fused with the transpose (warp-specialised)
+// ---------------------------------------------------------------------------
+// Compute warps (one row each at a time) and store warps of a variant.
+__host__ __device__ constexpr int xpose_compute_warps(bool dbl, int E) { return (E >= 24 || dbl) ? 4 : 8; }
+__host__ __device__ constexpr int xpose_store_warps(bool, int) { return 4; }
+
+// bounded mbarrier wait that also ends when the CTA aborts
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255) == 255 && *abort_flag) return false;
+    }
+    return false;
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <typename R, int SG, int E, int... Rs>
+__global__ void __launch_bounds__(32 * (xpose_compute_warps(sizeof(R) == 8, E) + xpose_store_warps(sizeof(R) == 8, E)), 1)
+    fft_tile_xpose_kernel(TArgs<R> A) {
+    typedef typename CT<R>::T C;
+    constexpr int M = (Rs * ... * 1);
+    static_assert(M == E * 32, "one warp per row");
+    static_assert(M % 16 == 0, "swizzles need 16-point blocks");
+    constexpr int ES = (int)sizeof(C);
+    constexpr int NCW = xpose_compute_warps(sizeof(R) == 8, E);
+    constexpr int NSW = xpose_store_warps(sizeof(R) == 8, E);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    // full[b]: the bulk copy into buffer b landed; done[b]: the NCW compute warps
+    // wrote its spectra; empty[b]: the NSW store warps have read it
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
+    uint64_t* done = full + 4;
+    uint64_t* empty = full + 8;
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + 96);
+    C* ring = reinterpret_cast<C*>(smem_raw + 128);
+    const int S = A.S, NST = A.nst;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lgS = __ffs(S) - 1;
+    const int lgNP = ES == 8 ? lgS - 1 : lgS;                 // log2 lanes per point of the read-out
+    const int lgsh = ES == 8 ? (4 - lgNP) : (3 - lgNP);       // read-out XOR step
+
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < NST; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&done[b], NCW);
+            mbar_init(&empty[b], NSW);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp < NCW) {
+        // ---- compute warps ----
+        int b = 0;
+        uint32_t par = 0;
+        for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+            if (!mbar_wait_or_abort(&full[b], par, abort_flag)) {
+                if (lane == 0) { atomicExch(A.status, 1); *abort_flag = 1; }
+                return;
+            }
+            i64 row0, rs;
+            int nrows, gi, u0, w;
+            tile_geom<R, true, M>(A, tile, row0, rs, nrows, gi, u0, w);
+            C* tb = ring + (i64)b * S * M;
+            for (int rl = warp; rl < nrows; rl += NCW) {
+                C* row = tb + rl * M;
+                C v[E];
+                tile_row_fft<R, SG, E, Rs...>(v, row, lane, A.tw);
+                __syncwarp();
+#pragma unroll
+                for (int q = 0; q < E; ++q) row[osw<ES>(rl, lane + 32 * q, lgsh)] = v[q];
+            }
+            // a bulk copy rewrites the slot after the store warps: order these writes first
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&done[b]);
+            if (++b == NST) { b = 0; par ^= 1; }
+        }
+        return;
+    }
+
+    // ---- store warps; the first one also issues the bulk copies ----
+    const int st = threadIdx.x - NCW * 32;             // 0 .. 32*NSW-1
+    const bool producer = warp == NCW;
+    uint32_t issued_par = 0;                            // bit b: parity of the last copy into buffer b
+    if (producer && lane == 0) {
+        for (int j = 0; j < NST; ++j) {
+            const i64 tj = blockIdx.x + (i64)j * gridDim.x;
+            if (tj < A.ntiles) tile_issue<R, true, M>(A, tj, ring + (i64)j * S * M, &full[j]);
+        }
+    }
+    const int lp = st & ((1 << lgNP) - 1);             // row pair (complex64) / row (complex128)
+    const int g0 = st >> lgNP;                          // first point of this thread
+    const int gstep = (32 * NSW) >> lgNP;
+    int b = 0;
+    uint32_t par = 0;
+    bool failed = false;
+    for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+        if (!mbar_wait_or_abort(&done[b], par, abort_flag)) { failed = true; break; }
+        i64 row0, rs;
+        int nrows, gi, u0, w;
+        tile_geom<R, true, M>(A, tile, row0, rs, nrows, gi, u0, w);
+        const C* tb = ring + (i64)b * S * M;
+        const FGroup& g = A.groups[gi];
+        for (int kk = 0; kk < g.nseg; ++kk) {
+            const FSeg sg = A.segs[g.seg_first + kk];
+            const int npts = sg.i1 - sg.i0;
+            C* dbase = A.out + sg.dst_off + (i64)w * sg.dw + u0;
+            if constexpr (ES == 8) {
+                const int r0 = 2 * lp;
+                if (r0 < nrows) {
+                    const bool two = r0 + 1 < nrows;
+                    const C* s0 = tb + r0 * M;
+                    const C* s1 = s0 + M;
+                    for (int ii = g0; ii < npts; ii += gstep) {
+                        const int i = sg.i0 + ii;
+                        const C a = s0[osw<ES>(r0, i, lgsh)];
+                        C* d = dbase + (i64)ii * sg.di + r0;
+                        if (two) {
+                            const C c = s1[osw<ES>(r0 + 1, i, lgsh)];
+                            if (A.pair_ok) {
+                                float4 q4;
+                                q4.x = a.x; q4.y = a.y; q4.z = c.x; q4.w = c.y;
+                                *reinterpret_cast<float4*>(d) = q4;
+                            } else {
+                                d[0] = a;
+                                d[1] = c;
+                            }
+                        } else {
+                            d[0] = a;
+                        }
+                    }
+                }
+            } else {
+                const int r0 = lp;
+                if (r0 < nrows) {
+                    const C* s0 = tb + r0 * M;
+                    for (int ii = g0; ii < npts; ii += gstep) {
+                        const int i = sg.i0 + ii;
+                        dbase[(i64)ii * sg.di + r0] = s0[osw<ES>(r0, i, lgsh)];
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[b]);
+        if (producer) {
+            // every store warp has read buffer b: refill it
+            if (!mbar_wait_or_abort(&empty[b], par, abort_flag)) { failed = true; break; }
+            if (lane == 0) {
+                const i64 tn = tile + (i64)NST * gridDim.x;
+                if (tn < A.ntiles) {
+                    tile_issue<R, true, M>(A, tn, const_cast<C*>(tb), &full[b]);
+                    issued_par = (issued_par & ~(1u << b)) | ((par ^ 1u) << b);
+                }
+            }
+            __syncwarp();
+        }
+        if (++b == NST) { b = 0; par ^= 1; }
+    }
+    if (failed) {
+        if (lane == 0) { atomicExch(A.status, 1); *abort_flag = 1; }
+        if (producer && lane == 0) {
+            // wait (bounded) for the last copy issued into every buffer; a copy
+            // that already landed completes its wait at once
+            for (int j = 0; j < NST && blockIdx.x + (i64)j * gridDim.x < A.ntiles; ++j)
+                mbar_wait_bounded(&full[j], (issued_par >> j) & 1u);
+        }
+    }
+}
+
+// Tile-kernel entry points of one precision (fft_tile_f32.cu / fft_tile_f64.cu):
+// nullptr when no variant is compiled for M.
+template <typename R>
+struct TilePtr {
+    static void* get(int M, int sign, bool xpose);
+    static int points_per_thread(int M);   // E of the compiled variant, 0 if none
+};
+
+}  // namespace gb

@@ -211,9 +211,12 @@ static dtfft_error_t build_ffts(Plan& p) {
 // A step that does not fit the fused kernel keeps the two-kernel form.
 static void build_fused(Plan& p) {
     if (p.transpose_only || p.kind == K_R2R || p.z_slab || p.y_slab) return;
-    // opt-in until the fused pass beats FFT + transpose on the target sizes
+    // Default: fuse where the warp-per-row tile kernel takes the rows (it beats
+    // FFT + transpose there).  DTFFT_GB_FUSE=1 also fuses the other lengths
+    // with the register kernels; DTFFT_GB_FUSE=0 keeps every step unfused.
     const char* fz = getenv("DTFFT_GB_FUSE");
-    if (!fz || strcmp(fz, "0") == 0) return;
+    if (fz && strcmp(fz, "0") == 0) return;
+    const bool tile_only = !(fz && strcmp(fz, "1") == 0);
     const int dbl = p.precision == DTFFT_DOUBLE ? 1 : 0;
     std::vector<std::pair<int, int>> steps;   // (transpose type, FFT dim on its send layout)
     if (p.ndims == 2) steps = {{1, 1}, {-1, 2}};
@@ -224,7 +227,7 @@ static void build_fused(Plan& p) {
         const BoxList& bl = p.tr[t + 3];
         if (bl.host.empty() || !p.fft[d - 1]) continue;
         FusedFT* f = nullptr;
-        if (FusedFT::create(bl, p.pen[d - 1].gsize[0], dbl, &f) == DTFFT_SUCCESS) p.ft[t + 3] = f;
+        if (FusedFT::create(bl, p.pen[d - 1].gsize[0], dbl, tile_only, &f) == DTFFT_SUCCESS) p.ft[t + 3] = f;
     }
 }
 
@@ -440,11 +443,11 @@ static dtfft_error_t run_execute(Plan& p, void* in, void* out, bool fwd, void* a
     if (p.ndims == 2 || p.y_slab) {
         if (p.transpose_only) return T(p, fwd ? 1 : -1, in, out);
         if (fwd) {
-            if (p.ft[1 + 3]) GB_TRY(p.ft[1 + 3]->execute(in, out, S, p.stream));   // fft(1) + X->Y
+            if (p.ft[1 + 3] && p.ft[1 + 3]->usable(in, out)) GB_TRY(p.ft[1 + 3]->execute(in, out, S, p.stream));   // fft(1) + X->Y
             else { GB_TRY(F(p, 1, in, aux, S)); GB_TRY(T(p, 1, aux, out)); }
             return F(p, 2, out, out, S);
         }
-        if (p.ft[-1 + 3]) GB_TRY(p.ft[-1 + 3]->execute(in, aux, S, p.stream));      // fft(2) + Y->X
+        if (p.ft[-1 + 3] && p.ft[-1 + 3]->usable(in, aux)) GB_TRY(p.ft[-1 + 3]->execute(in, aux, S, p.stream));      // fft(2) + Y->X
         else { GB_TRY(F(p, 2, in, in, S)); GB_TRY(T(p, -1, in, aux)); }
         return F(p, 1, aux, out, S);
     }
@@ -467,17 +470,17 @@ static dtfft_error_t run_execute(Plan& p, void* in, void* out, bool fwd, void* a
     // generic schedule; an FFT and the transpose after it run as one fused pass
     // when the plan built one (the buffer roles of the reference are kept)
     if (fwd) {
-        if (p.ft[1 + 3]) GB_TRY(p.ft[1 + 3]->execute(in, out, S, p.stream));       // fft(1) + X->Y
+        if (p.ft[1 + 3] && p.ft[1 + 3]->usable(in, out)) GB_TRY(p.ft[1 + 3]->execute(in, out, S, p.stream));       // fft(1) + X->Y
         else { GB_TRY(F(p, 1, in, aux, S)); GB_TRY(T(p, 1, aux, out)); }
-        if (p.ft[2 + 3]) GB_TRY(p.ft[2 + 3]->execute(out, aux, S, p.stream));      // fft(2) + Y->Z
+        if (p.ft[2 + 3] && p.ft[2 + 3]->usable(out, aux)) GB_TRY(p.ft[2 + 3]->execute(out, aux, S, p.stream));      // fft(2) + Y->Z
         else { GB_TRY(F(p, 2, out, out, S)); GB_TRY(T(p, 2, out, aux)); }
         return F(p, 3, aux, out, S);
     }
     void* cur;
-    if (p.ft[-2 + 3]) { GB_TRY(p.ft[-2 + 3]->execute(in, aux, S, p.stream)); cur = aux; }   // fft(3) + Z->Y
+    if (p.ft[-2 + 3] && p.ft[-2 + 3]->usable(in, aux)) { GB_TRY(p.ft[-2 + 3]->execute(in, aux, S, p.stream)); cur = aux; }   // fft(3) + Z->Y
     else { GB_TRY(F(p, 3, in, aux, S)); GB_TRY(T(p, -2, aux, in)); cur = in; }
     void* other = cur == aux ? in : aux;
-    if (p.ft[-1 + 3]) GB_TRY(p.ft[-1 + 3]->execute(cur, other, S, p.stream));             // fft(2) + Y->X
+    if (p.ft[-1 + 3] && p.ft[-1 + 3]->usable(cur, other)) GB_TRY(p.ft[-1 + 3]->execute(cur, other, S, p.stream));             // fft(2) + Y->X
     else { GB_TRY(F(p, 2, cur, cur, S)); GB_TRY(T(p, -1, cur, other)); }
     return F(p, 1, other, out, S);
 }

@@ -35,6 +35,12 @@ C2C_CASES = [
     ([96, 80, 64], [1, 1, 4], np.complex64),         # Z-slab on 4 ranks
     ([31, 44], [1, 3], np.complex64),
     ([512, 24], [1, 1], np.complex64),
+    # tile-kernel row lengths with a ragged last tile (rows % 16 != 0)
+    ([512, 7, 3], [1, 1, 1], np.complex64),
+    ([1024, 5, 3], [1, 1, 1], np.complex64),
+    ([768, 9, 2], [1, 1, 2], np.complex64),
+    ([256, 256, 3], [1, 1, 1], np.complex128),
+    ([512, 3, 5], [1, 1, 1], np.complex128),
 ]
 
 
@@ -66,6 +72,17 @@ def test_c2c_forward_backward(dt, orc, cuda, dims, grid, np_dtype):
     ([48, 36, 40], [1, 3, 2], np.complex128),
     ([96, 64], [1, 2], np.complex64),
     ([32, 24, 40], [1, 1, 1], np.float32),          # R2C: Y and Z axes fuse
+    # rows the warp-per-row tile kernel takes (M = 256 / 512 / 768 / 1024)
+    ([512, 512, 16], [1, 2, 2], np.complex64),
+    ([256, 256, 48], [1, 2, 4], np.complex64),
+    ([256, 40, 36], [1, 2, 2], np.complex64),        # ragged tiles: 20 and 18 rows per rank
+    ([256, 33, 21], [1, 2, 2], np.complex64),        # odd destination strides (8-byte stores)
+    ([768, 24, 20], [1, 2, 1], np.complex64),
+    ([1024, 16, 20], [1, 1, 2], np.complex64),
+    ([256, 256, 24], [1, 2, 2], np.complex128),
+    ([512, 40, 12], [1, 3, 1], np.complex128),
+    ([256, 512], [1, 2], np.complex64),
+    ([512, 256, 32], [1, 1, 1], np.float32),        # R2C: the Y axis (256) fuses
 ])
 def test_fused_fft_transpose(dt, orc, cuda, monkeypatch, dims, grid, np_dtype):
     """Plans built with the fused FFT + transpose passes (DTFFT_GB_FUSE=1)."""
