@@ -30,6 +30,7 @@ struct Plan {
     int grid[3] = {1, 1, 1};
     int P = 1;
     bool z_slab = false, y_slab = false;
+    bool zs_generic = false;    // Z-slab C2C plan executed through the fused generic schedule
     Layout pen[3];
     Layout real_x;              // R2C: real X pencils
     bool user = false;          // built from every virtual rank's own block
@@ -163,14 +164,11 @@ static dtfft_error_t build_reshapes(Plan& p) {
     return DTFFT_SUCCESS;
 }
 
-// FFT plans per aligned dim (src/dtfft_plan.F90:2381-2653)
-static dtfft_error_t build_ffts(Plan& p) {
-    if (p.transpose_only) return DTFFT_SUCCESS;
-    const int nd = p.ndims;
+// FFT plan along aligned dim d (2D over the slab's two dims with two_d)
+// (src/dtfft_plan.F90:2381-2653)
+static dtfft_error_t build_fft(Plan& p, int d, bool two_d) {
     const int dbl = p.precision == DTFFT_DOUBLE ? 1 : 0;
-    for (int d = 1; d <= nd; ++d) {
-        if ((p.z_slab && d == 2) || (p.y_slab && d == 3)) continue;
-        const bool two_d = (p.z_slab && d == 1) || (p.y_slab && d == 2);
+    {
         FftDesc fd;
         fd.dbl = dbl;
         fd.rank = two_d ? 2 : 1;
@@ -202,20 +200,33 @@ static dtfft_error_t build_ffts(Plan& p) {
                 fd.kind_fast = p.kinds[d - 1];
             }
         }
+        delete p.fft[d - 1];
+        p.fft[d - 1] = nullptr;
         GB_TRY(FftPlan::create(fd, &p.fft[d - 1]));
+    }
+    return DTFFT_SUCCESS;
+}
+
+static dtfft_error_t build_ffts(Plan& p) {
+    if (p.transpose_only) return DTFFT_SUCCESS;
+    for (int d = 1; d <= p.ndims; ++d) {
+        if ((p.z_slab && d == 2) || (p.y_slab && d == 3)) continue;
+        GB_TRY(build_fft(p, d, (p.z_slab && d == 1) || (p.y_slab && d == 2)));
     }
     return DTFFT_SUCCESS;
 }
 
 // Fused FFT + transpose steps of the generic and 2D schedules (C2C axes only).
 // A step that does not fit the fused kernel keeps the two-kernel form.
-static void build_fused(Plan& p) {
-    if (p.transpose_only || p.kind == K_R2R || p.z_slab || p.y_slab) return;
+static dtfft_error_t build_fused(Plan& p) {
+    if (p.transpose_only || p.kind == K_R2R || p.y_slab) return DTFFT_SUCCESS;
+    if (p.z_slab && (p.kind != K_C2C || p.reshape || p.ndims != 3)) return DTFFT_SUCCESS;
     // Default: fuse where the warp-per-row tile kernel takes the rows (it beats
     // FFT + transpose there).  DTFFT_GB_FUSE=1 also fuses the other lengths
     // with the register kernels; DTFFT_GB_FUSE=0 keeps every step unfused.
+    // The tensor-core form (fft_form() == 1) keeps its row passes unfused.
     const char* fz = getenv("DTFFT_GB_FUSE");
-    if (fz && strcmp(fz, "0") == 0) return;
+    if ((fz && strcmp(fz, "0") == 0) || fft_form() == 1) return DTFFT_SUCCESS;
     const bool tile_only = !(fz && strcmp(fz, "1") == 0);
     const int dbl = p.precision == DTFFT_DOUBLE ? 1 : 0;
     std::vector<std::pair<int, int>> steps;   // (transpose type, FFT dim on its send layout)
@@ -225,10 +236,28 @@ static void build_fused(Plan& p) {
         const int t = st.first, d = st.second;
         if (p.kind == K_R2C && d == 1) continue;   // the X axis is R2C
         const BoxList& bl = p.tr[t + 3];
-        if (bl.host.empty() || !p.fft[d - 1]) continue;
+        if (bl.host.empty() || (!p.fft[d - 1] && !p.z_slab)) continue;
         FusedFT* f = nullptr;
-        if (FusedFT::create(bl, p.pen[d - 1].gsize[0], dbl, tile_only, &f) == DTFFT_SUCCESS) p.ft[t + 3] = f;
+        if (FusedFT::create(bl, p.pen[d - 1].gsize[0], dbl, p.z_slab || tile_only, &f) == DTFFT_SUCCESS)
+            p.ft[t + 3] = f;
     }
+    if (!p.z_slab) return DTFFT_SUCCESS;
+    // A Z-slab C2C plan on one GPU: when all four FFT + transpose passes fuse,
+    // the generic X -> Y -> Z schedule moves the data three times per
+    // direction instead of the slab's four (2D FFT = rows + strided columns,
+    // X -> Z, Z rows), with the same result in the same Z-pencil layout.
+    bool all = true;
+    for (auto st : steps) all = all && p.ft[st.first + 3] != nullptr;
+    if (all && build_fft(p, 1, false) == DTFFT_SUCCESS && build_fft(p, 2, false) == DTFFT_SUCCESS) {
+        p.zs_generic = true;
+        return DTFFT_SUCCESS;
+    }
+    for (auto st : steps) { delete p.ft[st.first + 3]; p.ft[st.first + 3] = nullptr; }
+    if (!all) return DTFFT_SUCCESS;
+    // the rank-1 plans could not be built: back to the slab's 2D plan
+    delete p.fft[1];
+    p.fft[1] = nullptr;
+    return build_fft(p, 1, true);
 }
 
 static dtfft_error_t create_plan(int kind, int8_t ndims, const int32_t* dims, const int32_t* kinds,
@@ -303,7 +332,7 @@ static dtfft_error_t create_plan(int kind, int8_t ndims, const int32_t* dims, co
     if (e == DTFFT_SUCCESS) e = build_transposes(*p);
     if (e == DTFFT_SUCCESS) e = build_reshapes(*p);
     if (e == DTFFT_SUCCESS) e = build_ffts(*p);
-    if (e == DTFFT_SUCCESS) build_fused(*p);
+    if (e == DTFFT_SUCCESS) e = build_fused(*p);
     if (e == DTFFT_SUCCESS && (effort == DTFFT_EXHAUSTIVE || cfg.enable_kernel_autotune)) {
         for (auto& bl : p->tr) {
             if (bl.host.empty()) continue;
@@ -436,22 +465,42 @@ static dtfft_error_t run_execute_reshape(Plan& p, void* in, void* out, bool fwd,
     return RS(p, XP2B, aux, out);
 }
 
-// execute_2d / execute_z_slab / execute_generic (src/dtfft_plan.F90:877-1101)
+// FFT along the send layout of transpose t followed by transpose t, from
+// `src` to `dst`: one fused pass when the plan built one and it can run on
+// these buffers, else FFT in place on `src` then the transpose.  `src` is
+// clobbered either way.
+static dtfft_error_t FT(Plan& p, int t, void* src, void* dst, int S) {
+    FusedFT* f = p.ft[t + 3];
+    if (f && f->usable(src, dst)) return f->execute(src, dst, S, p.stream);
+    const int d = t == 1 ? 1 : (t == 2 || t == -1) ? 2 : 3;
+    GB_TRY(F(p, d, src, src, S));
+    return T(p, t, src, dst);
+}
+static bool fused(const Plan& p, int t) { return p.ft[t + 3] != nullptr; }
+
+// execute_2d / execute_z_slab / execute_generic (src/dtfft_plan.F90:877-1101).
+// Buffer roles follow the reference's: `in` may be clobbered by the backward
+// direction, `aux` holds intermediate layouts, and in == out is allowed.
 static dtfft_error_t run_execute(Plan& p, void* in, void* out, bool fwd, void* aux, bool inplace) {
     if (p.reshape) return run_execute_reshape(p, in, out, fwd, aux);
     const int S = fwd ? FFT_FWD : FFT_BWD;
     if (p.ndims == 2 || p.y_slab) {
         if (p.transpose_only) return T(p, fwd ? 1 : -1, in, out);
         if (fwd) {
-            if (p.ft[1 + 3] && p.ft[1 + 3]->usable(in, out)) GB_TRY(p.ft[1 + 3]->execute(in, out, S, p.stream));   // fft(1) + X->Y
-            else { GB_TRY(F(p, 1, in, aux, S)); GB_TRY(T(p, 1, aux, out)); }
+            // fft(1) + X->Y, then fft(2) in place
+            if (fused(p, 1)) {
+                void* y = inplace ? aux : out;
+                GB_TRY(FT(p, 1, in, y, S));
+                return F(p, 2, y, out, S);
+            }
+            GB_TRY(F(p, 1, in, aux, S));
+            GB_TRY(T(p, 1, aux, out));
             return F(p, 2, out, out, S);
         }
-        if (p.ft[-1 + 3] && p.ft[-1 + 3]->usable(in, aux)) GB_TRY(p.ft[-1 + 3]->execute(in, aux, S, p.stream));      // fft(2) + Y->X
-        else { GB_TRY(F(p, 2, in, in, S)); GB_TRY(T(p, -1, in, aux)); }
+        GB_TRY(FT(p, -1, in, aux, S));   // fft(2) + Y->X
         return F(p, 1, aux, out, S);
     }
-    if (p.z_slab && !(p.transpose_only && inplace)) {
+    if (p.z_slab && !p.zs_generic && !(p.transpose_only && inplace)) {
         if (p.transpose_only) return T(p, fwd ? 3 : -3, in, out);
         if (fwd) {
             GB_TRY(F(p, 1, in, aux, S));
@@ -467,22 +516,22 @@ static dtfft_error_t run_execute(Plan& p, void* in, void* out, bool fwd, void* a
         GB_TRY(T(p, -2, in, aux));
         return T(p, -1, aux, out);
     }
-    // generic schedule; an FFT and the transpose after it run as one fused pass
-    // when the plan built one (the buffer roles of the reference are kept)
+    // generic schedule (also the single-GPU route of Z-slab C2C plans whose
+    // passes all fuse: three HBM passes instead of the slab's four)
     if (fwd) {
-        if (p.ft[1 + 3] && p.ft[1 + 3]->usable(in, out)) GB_TRY(p.ft[1 + 3]->execute(in, out, S, p.stream));       // fft(1) + X->Y
-        else { GB_TRY(F(p, 1, in, aux, S)); GB_TRY(T(p, 1, aux, out)); }
-        if (p.ft[2 + 3] && p.ft[2 + 3]->usable(out, aux)) GB_TRY(p.ft[2 + 3]->execute(out, aux, S, p.stream));      // fft(2) + Y->Z
-        else { GB_TRY(F(p, 2, out, out, S)); GB_TRY(T(p, 2, out, aux)); }
-        return F(p, 3, aux, out, S);
+        void* y;                                   // Y-pencil data after fft(1) + X->Y
+        if (fused(p, 1)) { y = inplace ? aux : out; GB_TRY(FT(p, 1, in, y, S)); }
+        else { GB_TRY(F(p, 1, in, aux, S)); GB_TRY(T(p, 1, aux, out)); y = out; }
+        void* z = y == aux ? out : aux;            // Z-pencil data after fft(2) + Y->Z
+        GB_TRY(FT(p, 2, y, z, S));
+        return F(p, 3, z, out, S);
     }
-    void* cur;
-    if (p.ft[-2 + 3] && p.ft[-2 + 3]->usable(in, aux)) { GB_TRY(p.ft[-2 + 3]->execute(in, aux, S, p.stream)); cur = aux; }   // fft(3) + Z->Y
-    else { GB_TRY(F(p, 3, in, aux, S)); GB_TRY(T(p, -2, aux, in)); cur = in; }
-    void* other = cur == aux ? in : aux;
-    if (p.ft[-1 + 3] && p.ft[-1 + 3]->usable(cur, other)) GB_TRY(p.ft[-1 + 3]->execute(cur, other, S, p.stream));             // fft(2) + Y->X
-    else { GB_TRY(F(p, 2, cur, cur, S)); GB_TRY(T(p, -1, cur, other)); }
-    return F(p, 1, other, out, S);
+    void* y;                                       // Y-pencil data after fft(3) + Z->Y
+    if (fused(p, -2)) { y = aux; GB_TRY(FT(p, -2, in, aux, S)); }
+    else { GB_TRY(F(p, 3, in, aux, S)); GB_TRY(T(p, -2, aux, in)); y = in; }
+    void* x = y == aux ? in : aux;                 // X-pencil data after fft(2) + Y->X
+    GB_TRY(FT(p, -1, y, x, S));
+    return F(p, 1, x, out, S);
 }
 
 struct Request { uint32_t magic; int type; };

@@ -113,6 +113,35 @@ def test_fused_fft_transpose(dt, orc, cuda, monkeypatch, dims, grid, np_dtype):
     plan.destroy()
 
 
+@pytest.mark.parametrize("dims,grid,np_dtype,inplace", [
+    ([256, 256, 256], [1, 1, 1], np.complex64, False),   # Z-slab plan, all three axes on tile kernels
+    ([256, 256, 256], [1, 1, 1], np.complex64, True),
+    ([256, 512, 256], [1, 1, 2], np.complex128, False),  # Z-slab on two virtual ranks
+    ([512, 256, 48], [1, 2, 2], np.complex64, True),     # generic schedule, in == out
+    ([256, 512], [1, 2], np.complex64, True),            # 2D, in == out
+])
+def test_tile_schedules(dt, orc, cuda, dims, grid, np_dtype, inplace):
+    """Fused tile passes on the default path: Z-slab plans take the generic
+    X -> Y -> Z route when every pass fuses, and in-place execution (in ==
+    out) never lets a fused pass read and write the same buffer."""
+    nd = len(dims)
+    plan = dt.PlanC2C(dims, comm=comm_for(dt, grid), precision=_prec(dt, np_dtype), executor=dt.Executor.CUFFT)
+    if nd == 3 and grid[1] == 1:
+        assert plan.z_slab_enabled
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=7)
+    x = orc.global_to_packed(g, nd, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = a if inplace else empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    expect = orc.global_to_packed(orc.forward_values(g, "c2c"), nd, grid, _final_layout(plan, nd))
+    assert orc.rel_l2(from_dev(b, expect.size, np_dtype), expect) <= TOL[np_dtype]
+    c = b if inplace else empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    back = from_dev(c, x.size, np_dtype).astype(np.complex128) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= TOL[np_dtype]
+    plan.destroy()
+
+
 def test_c2c_schedules_agree(dt, orc, cuda):
     """Z-slab, Y-slab and the generic 3-pencil schedule give the same spectrum."""
     dims = [64, 64, 64]
