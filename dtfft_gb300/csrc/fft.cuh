@@ -92,7 +92,7 @@ private:
     int pipe_per_sm_ = 0;
     // warp-per-row tile kernel (fft_tile.cuh): used when tile_ is set
     bool tile_ = false;
-    int tile_nst_ = 0, tile_threads_ = 0, pair_ok_ = 0;
+    int tile_nst_ = 0, tile_threads_ = 0, pair_ok_ = 0, ncw_ = 0, nsw_ = 0;
     const void* tw_bwd_ = nullptr;
     Schedule sched_;
     const void* tw_ = nullptr;

@@ -72,7 +72,7 @@ struct FftStep {
     bool reads_out = false;  // step reads the plan's output buffer (second pass)
     void* tc = nullptr;      // tensor-core form of this step (C2C FP32 rows), see fft_tc.cu
     bool tile = false;       // C2C rows: warp-per-row tile kernel (fft_tile.cuh)
-    int tile_S = 0, tile_nst = 0, tile_threads = 0;
+    int tile_S = 0, tile_nst = 0, tile_threads = 0, tile_nw = 0;
     size_t tile_smem = 0;
     const void* tw_dir = nullptr;   // W_m^(sign*e) for this step's direction
     ~FftStep() { tc_destroy(tc); }
@@ -230,8 +230,8 @@ static bool tile_shape(int m, int dbl, bool xpose, TileShape& ts) {
     const int nst = (int)std::min<size_t>(4, (cap - 128) / tile);
     if (nst < 2) return false;
     ts.E = E; ts.S = S; ts.nst = nst;
-    if (xpose) ts.threads = 32 * (xpose_compute_warps(dbl != 0, E) + xpose_store_warps(dbl != 0, E));
-    else ts.threads = 32 * std::min(S, tile_threads(dbl != 0, E) / 32);
+    ts.threads = dbl ? TilePtr<double>::default_threads(m, xpose) : TilePtr<float>::default_threads(m, xpose);
+    if (!xpose) ts.threads = std::min(ts.threads, 32 * S);
     ts.smem = 128 + (size_t)nst * tile;
     return true;
 }
@@ -317,10 +317,17 @@ static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
     if (!S.cols && S.mode == M_C2C && S.idist == m && S.odist == m) {
         TileShape ts;
         if (tile_shape(m, S.dbl, false, ts)) {
-            const void* fn = S.dbl ? TilePtr<double>::get(m, sign, false) : TilePtr<float>::get(m, sign, false);
+            int nw = 0;
+            if (const char* tw_env = getenv("DTFFT_GB_TILE_WARPS")) {   // experiments
+                const int w = atoi(tw_env);
+                if (w > 0 && (S.dbl ? TilePtr<double>::get(m, sign, false, w) : TilePtr<float>::get(m, sign, false, w)))
+                    nw = w;
+            }
+            const void* fn = S.dbl ? TilePtr<double>::get(m, sign, false, nw) : TilePtr<float>::get(m, sign, false, nw);
             if (fn && set_smem_attrs(fn, ts.smem) == DTFFT_SUCCESS) {
                 S.tile = true;
-                S.tile_S = ts.S; S.tile_nst = ts.nst; S.tile_threads = ts.threads; S.tile_smem = ts.smem;
+                S.tile_S = ts.S; S.tile_nst = ts.nst; S.tile_threads = nw ? 32 * nw : ts.threads; S.tile_smem = ts.smem;
+                S.tile_nw = nw;
                 GB_TRY(upload_dir_table(m, sign, S.dbl, owned, &S.tw_dir));
             }
         }
@@ -428,7 +435,7 @@ static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, 
         P.nsig = S.nsig; P.groups = nullptr; P.segs = nullptr; P.ngroups = 0;
         P.ntiles = (S.nsig + S.tile_S - 1) / S.tile_S;
         P.S = S.tile_S; P.nst = S.tile_nst; P.pair_ok = 0; P.status = status_ptr();
-        void (*kfn)(TArgs<R>) = (void (*)(TArgs<R>))TilePtr<R>::get(S.m, S.sign, false);
+        void (*kfn)(TArgs<R>) = (void (*)(TArgs<R>))TilePtr<R>::get(S.m, S.sign, false, S.tile_nw);
         if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
         const i64 grid = std::min<i64>(P.ntiles, (i64)sm_count());
         if (grid <= 0) return DTFFT_SUCCESS;
@@ -671,10 +678,20 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
         int pair = dbl ? 0 : 1;
         for (const FSeg& sgm : segs) pair = pair && (sgm.dst_off % 2 == 0) && (sgm.di % 2 == 0) && (sgm.dw % 2 == 0);
         p->pair_ok_ = pair;
+        // warp split override of the fused pass (experiments): DTFFT_GB_XPOSE_WARPS=<compute>,<store>
+        if (const char* xw = getenv("DTFFT_GB_XPOSE_WARPS")) {
+            int c = 0, w = 0;
+            if (sscanf(xw, "%d,%d", &c, &w) == 2 && (dbl ? TilePtr<double>::get(m, -1, true, c, w)
+                                                           : TilePtr<float>::get(m, -1, true, c, w))) {
+                p->ncw_ = c; p->nsw_ = w;
+                p->tile_threads_ = 32 * (c + w);
+            }
+        }
         err = upload_dir_table(m, -1, dbl, p->owned_, &p->tw_);
         if (err == DTFFT_SUCCESS) err = upload_dir_table(m, 1, dbl, p->owned_, &p->tw_bwd_);
         for (int sg = -1; sg <= 1 && err == DTFFT_SUCCESS; sg += 2) {
-            const void* fn = dbl ? TilePtr<double>::get(m, sg, true) : TilePtr<float>::get(m, sg, true);
+            const void* fn = dbl ? TilePtr<double>::get(m, sg, true, p->ncw_, p->nsw_)
+                                 : TilePtr<float>::get(m, sg, true, p->ncw_, p->nsw_);
             err = set_smem_attrs(fn, ts.smem);
         }
     } else {
@@ -757,15 +774,15 @@ static dtfft_error_t launch_fused_pipe(int m, int E, int T, int S, int pitch, co
 }
 
 template <typename R>
-static dtfft_error_t launch_fused_tile(int m, int S, int nst, int threads, size_t smem, int pair_ok, const void* tw,
-                                      const void* groups, const void* segs, int ngroups, i64 tiles, const void* in,
-                                      void* out, int sign, cudaStream_t s) {
+static dtfft_error_t launch_fused_tile(int m, int S, int nst, int threads, int ncw, int nsw, size_t smem, int pair_ok,
+                                      const void* tw, const void* groups, const void* segs, int ngroups, i64 tiles,
+                                      const void* in, void* out, int sign, cudaStream_t s) {
     typedef typename CT<R>::T C;
     TArgs<R> P;
     P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)tw;
     P.nsig = 0; P.groups = (const FGroup*)groups; P.segs = (const FSeg*)segs; P.ngroups = ngroups;
     P.ntiles = tiles; P.S = S; P.nst = nst; P.pair_ok = pair_ok; P.status = status_ptr();
-    void (*kfn)(TArgs<R>) = (void (*)(TArgs<R>))TilePtr<R>::get(m, sign, true);
+    void (*kfn)(TArgs<R>) = (void (*)(TArgs<R>))TilePtr<R>::get(m, sign, true, ncw, nsw);
     if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     const i64 grid = std::min<i64>(tiles, (i64)sm_count());
     void* tok = prof_begin(s);
@@ -782,10 +799,10 @@ dtfft_error_t FusedFT::execute(const void* in, void* out, int sign, cudaStream_t
         if (((uintptr_t)in % 16) != 0 || ((uintptr_t)out % 16) != 0) return DTFFT_ERROR_INVALID_USAGE;
         const void* tw = sign > 0 ? tw_bwd_ : tw_;
         if (dbl_)
-            return launch_fused_tile<double>(m_, S_, tile_nst_, tile_threads_, smem_, pair_ok_, tw, groups_, segs_,
-                                             ngroups_, ctas_, in, out, sign, s);
-        return launch_fused_tile<float>(m_, S_, tile_nst_, tile_threads_, smem_, pair_ok_, tw, groups_, segs_,
-                                        ngroups_, ctas_, in, out, sign, s);
+            return launch_fused_tile<double>(m_, S_, tile_nst_, tile_threads_, ncw_, nsw_, smem_, pair_ok_, tw, groups_,
+                                             segs_, ngroups_, ctas_, in, out, sign, s);
+        return launch_fused_tile<float>(m_, S_, tile_nst_, tile_threads_, ncw_, nsw_, smem_, pair_ok_, tw, groups_,
+                                        segs_, ngroups_, ctas_, in, out, sign, s);
     }
     if (pipe_per_sm_ > 0 && ((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
         if (dbl_)

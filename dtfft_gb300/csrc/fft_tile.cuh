@@ -167,10 +167,8 @@ __device__ __forceinline__ void tile_row_fft(typename CT<R>::T (&v)[E], typename
 // ---------------------------------------------------------------------------
 // Plain rows
 // ---------------------------------------------------------------------------
-__host__ __device__ constexpr int tile_threads(bool dbl, int E) { return (E >= 16 || dbl) ? 256 : 512; }
-
-template <typename R, int SG, int E, int... Rs>
-__global__ void __launch_bounds__(tile_threads(sizeof(R) == 8, E), 1) fft_tile_kernel(TArgs<R> A) {
+template <typename R, int SG, int NW, int E, int... Rs>
+__global__ void __launch_bounds__(32 * NW, 1) fft_tile_kernel(TArgs<R> A) {
     typedef typename CT<R>::T C;
     constexpr int M = (Rs * ... * 1);
     static_assert(M == E * 32, "one warp per row");
@@ -236,10 +234,6 @@ __global__ void __launch_bounds__(tile_threads(sizeof(R) == 8, E), 1) fft_tile_k
 // ---------------------------------------------------------------------------
 // Rows fused with the transpose (warp-specialised)
 // ---------------------------------------------------------------------------
-// Compute warps (one row each at a time) and store warps of a variant.
-__host__ __device__ constexpr int xpose_compute_warps(bool dbl, int E) { return (E >= 24 || dbl) ? 4 : 8; }
-__host__ __device__ constexpr int xpose_store_warps(bool, int) { return 4; }
-
 // bounded mbarrier wait that also ends when the CTA aborts
 __device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
     for (int it = 0; it < (1 << 22); ++it) {
@@ -252,16 +246,13 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-template <typename R, int SG, int E, int... Rs>
-__global__ void __launch_bounds__(32 * (xpose_compute_warps(sizeof(R) == 8, E) + xpose_store_warps(sizeof(R) == 8, E)), 1)
-    fft_tile_xpose_kernel(TArgs<R> A) {
+template <typename R, int SG, int NCW, int NSW, int E, int... Rs>
+__global__ void __launch_bounds__(32 * (NCW + NSW), 1) fft_tile_xpose_kernel(TArgs<R> A) {
     typedef typename CT<R>::T C;
     constexpr int M = (Rs * ... * 1);
     static_assert(M == E * 32, "one warp per row");
     static_assert(M % 16 == 0, "swizzles need 16-point blocks");
     constexpr int ES = (int)sizeof(C);
-    constexpr int NCW = xpose_compute_warps(sizeof(R) == 8, E);
-    constexpr int NSW = xpose_store_warps(sizeof(R) == 8, E);
     extern __shared__ __align__(128) unsigned char smem_raw[];
     // full[b]: the bulk copy into buffer b landed; done[b]: the NCW compute warps
     // wrote its spectra; empty[b]: the NSW store warps have read it
@@ -350,6 +341,7 @@ __global__ void __launch_bounds__(32 * (xpose_compute_warps(sizeof(R) == 8, E) +
                     const bool two = r0 + 1 < nrows;
                     const C* s0 = tb + r0 * M;
                     const C* s1 = s0 + M;
+#pragma unroll 4
                     for (int ii = g0; ii < npts; ii += gstep) {
                         const int i = sg.i0 + ii;
                         const C a = s0[osw<ES>(r0, i, lgsh)];
@@ -411,8 +403,11 @@ __global__ void __launch_bounds__(32 * (xpose_compute_warps(sizeof(R) == 8, E) +
 // nullptr when no variant is compiled for M.
 template <typename R>
 struct TilePtr {
-    static void* get(int M, int sign, bool xpose);
-    static int points_per_thread(int M);   // E of the compiled variant, 0 if none
+    // kernel for rows of M points; ncw/nsw select a compiled warp split
+    // (plain: ncw = warps), 0 the default
+    static void* get(int M, int sign, bool xpose, int ncw = 0, int nsw = 0);
+    static int points_per_thread(int M);   // E of the compiled variants, 0 if none
+    static int default_threads(int M, bool xpose);
 };
 
 }  // namespace gb

@@ -3,33 +3,42 @@
 
 namespace gb {
 
-template <int SG>
-static void* tile_plain_f32(int M) {
-    switch (M) {
-    case 256: return (void*)fft_tile_kernel<float, SG, 8, 8, 8, 4>;
-    case 512: return (void*)fft_tile_kernel<float, SG, 16, 16, 16, 2>;
-    case 768: return (void*)fft_tile_kernel<float, SG, 24, 8, 8, 4, 3>;
-    case 1024: return (void*)fft_tile_kernel<float, SG, 32, 16, 16, 4>;
-    }
-    return nullptr;
-}
-
-template <int SG>
-static void* tile_xpose_f32(int M) {
-    switch (M) {
-    case 256: return (void*)fft_tile_xpose_kernel<float, SG, 8, 8, 8, 4>;
-    case 512: return (void*)fft_tile_xpose_kernel<float, SG, 16, 16, 16, 2>;
-    case 768: return (void*)fft_tile_xpose_kernel<float, SG, 24, 8, 8, 4, 3>;
-    case 1024: return (void*)fft_tile_xpose_kernel<float, SG, 32, 16, 16, 4>;
-    }
-    return nullptr;
-}
+// Warp counts compiled per row length: the first entry is the default, the
+// others are selectable for measurements (DTFFT_GB_TILE_WARPS = <warps>,
+// DTFFT_GB_XPOSE_WARPS = <compute>,<store>).
+#define GB_PLAIN(NW_, E_, ...)                                                                   \
+    if (nw == NW_ || (nw == 0 && first)) return sign < 0 ? (void*)fft_tile_kernel<float, -1, NW_, E_, __VA_ARGS__> \
+                                                        : (void*)fft_tile_kernel<float, 1, NW_, E_, __VA_ARGS__>;  \
+    first = false;
+#define GB_XPOSE(C_, S_, E_, ...)                                                                \
+    if ((ncw == C_ && nsw == S_) || (ncw == 0 && first))                                         \
+        return sign < 0 ? (void*)fft_tile_xpose_kernel<float, -1, C_, S_, E_, __VA_ARGS__>       \
+                        : (void*)fft_tile_xpose_kernel<float, 1, C_, S_, E_, __VA_ARGS__>;       \
+    first = false;
 
 template <>
-void* TilePtr<float>::get(int M, int sign, bool xpose) {
-    if (sign < 0) return xpose ? tile_xpose_f32<-1>(M) : tile_plain_f32<-1>(M);
-    return xpose ? tile_xpose_f32<1>(M) : tile_plain_f32<1>(M);
+void* TilePtr<float>::get(int M, int sign, bool xpose, int ncw, int nsw) {
+    bool first = true;
+    const int nw = ncw;
+    if (!xpose) {
+        switch (M) {
+        case 256: GB_PLAIN(4, 8, 8, 8, 4) GB_PLAIN(8, 8, 8, 8, 4) break;
+        case 512: GB_PLAIN(4, 16, 16, 16, 2) GB_PLAIN(8, 16, 16, 16, 2) break;
+        case 768: GB_PLAIN(8, 24, 8, 8, 4, 3) GB_PLAIN(4, 24, 8, 8, 4, 3) break;
+        case 1024: GB_PLAIN(8, 32, 16, 16, 4) GB_PLAIN(4, 32, 16, 16, 4) break;
+        }
+        return nullptr;
+    }
+    switch (M) {
+    case 256: GB_XPOSE(3, 5, 8, 8, 8, 4) GB_XPOSE(4, 4, 8, 8, 8, 4) break;
+    case 512: GB_XPOSE(3, 5, 16, 16, 16, 2) GB_XPOSE(4, 4, 16, 16, 16, 2) break;
+    case 768: GB_XPOSE(4, 4, 24, 8, 8, 4, 3) GB_XPOSE(3, 5, 24, 8, 8, 4, 3) break;
+    case 1024: GB_XPOSE(4, 4, 32, 16, 16, 4) GB_XPOSE(3, 5, 32, 16, 16, 4) break;
+    }
+    return nullptr;
 }
+#undef GB_PLAIN
+#undef GB_XPOSE
 
 template <>
 int TilePtr<float>::points_per_thread(int M) {
@@ -38,6 +47,18 @@ int TilePtr<float>::points_per_thread(int M) {
     case 512: return 16;
     case 768: return 24;
     case 1024: return 32;
+    }
+    return 0;
+}
+
+// Threads of the default variant.
+template <>
+int TilePtr<float>::default_threads(int M, bool xpose) {
+    switch (M) {
+    case 256: return xpose ? 32 * 8 : 32 * 4;
+    case 512: return xpose ? 32 * 8 : 32 * 4;
+    case 768: return xpose ? 32 * 8 : 32 * 8;
+    case 1024: return xpose ? 32 * 8 : 32 * 8;
     }
     return 0;
 }

@@ -3,28 +3,21 @@
 
 namespace gb {
 
-template <int SG>
-static void* tile_plain_f64(int M) {
-    switch (M) {
-    case 256: return (void*)fft_tile_kernel<double, SG, 8, 8, 8, 4>;
-    case 512: return (void*)fft_tile_kernel<double, SG, 16, 16, 16, 2>;
-    }
-    return nullptr;
-}
-
-template <int SG>
-static void* tile_xpose_f64(int M) {
-    switch (M) {
-    case 256: return (void*)fft_tile_xpose_kernel<double, SG, 8, 8, 8, 4>;
-    case 512: return (void*)fft_tile_xpose_kernel<double, SG, 16, 16, 16, 2>;
-    }
-    return nullptr;
-}
-
 template <>
-void* TilePtr<double>::get(int M, int sign, bool xpose) {
-    if (sign < 0) return xpose ? tile_xpose_f64<-1>(M) : tile_plain_f64<-1>(M);
-    return xpose ? tile_xpose_f64<1>(M) : tile_plain_f64<1>(M);
+void* TilePtr<double>::get(int M, int sign, bool xpose, int ncw, int nsw) {
+    (void)ncw; (void)nsw;
+    if (!xpose) {
+        switch (M) {
+        case 256: return sign < 0 ? (void*)fft_tile_kernel<double, -1, 8, 8, 8, 8, 4> : (void*)fft_tile_kernel<double, 1, 8, 8, 8, 8, 4>;
+        case 512: return sign < 0 ? (void*)fft_tile_kernel<double, -1, 8, 16, 16, 16, 2> : (void*)fft_tile_kernel<double, 1, 8, 16, 16, 16, 2>;
+        }
+        return nullptr;
+    }
+    switch (M) {
+    case 256: return sign < 0 ? (void*)fft_tile_xpose_kernel<double, -1, 4, 4, 8, 8, 8, 4> : (void*)fft_tile_xpose_kernel<double, 1, 4, 4, 8, 8, 8, 4>;
+    case 512: return sign < 0 ? (void*)fft_tile_xpose_kernel<double, -1, 4, 4, 16, 16, 16, 2> : (void*)fft_tile_xpose_kernel<double, 1, 4, 4, 16, 16, 16, 2>;
+    }
+    return nullptr;
 }
 
 template <>
@@ -32,6 +25,15 @@ int TilePtr<double>::points_per_thread(int M) {
     switch (M) {
     case 256: return 8;
     case 512: return 16;
+    }
+    return 0;
+}
+
+template <>
+int TilePtr<double>::default_threads(int M, bool xpose) {
+    (void)xpose;
+    switch (M) {
+    case 256: case 512: return 256;
     }
     return 0;
 }
