@@ -367,6 +367,125 @@ def tensor_core_section(args, dt, dev, stream, sizes=(768, 1024)):
     return out
 
 
+def config1_section(args, dt, dev, stream):
+    """2D C2C complex128 256x256 in one process (execute_2d: FFT X, X->Y, FFT Y
+    and back), inputs uniform[-1,1) re/im: fwd+bwd cycles/s with one
+    dtfft_execute per direction, and the same cycle replayed as one CUDA graph
+    per direction (dtfft_gb_batch_execute of this one plan).  1 MiB per buffer:
+    the cycle is launch- and L2-bound, not HBM-bound."""
+    import torch
+    dims = [256, 256]
+    plan = dt.PlanC2C(dims, precision=dt.Precision.DOUBLE, executor=dt.Executor.CUFFT,
+                      config=dt.Config(stream=stream.cuda_stream))
+    dt.set_config(dt.Config())
+    n = plan.alloc_size
+    g = torch.Generator(device=dev)
+    g.manual_seed(1)
+    x0 = torch.complex(torch.rand(n, device=dev, generator=g, dtype=torch.float64) * 2 - 1,
+                       torch.rand(n, device=dev, generator=g, dtype=torch.float64) * 2 - 1)
+    a = x0.clone()
+    b = torch.empty_like(a)
+    aux = torch.empty_like(a)
+    torch.cuda.synchronize()
+    plan.execute(a, b, dt.Execute.FORWARD, aux)
+    plan.execute(b, a, dt.Execute.BACKWARD, aux)
+    torch.cuda.synchronize()
+    rt = float(torch.linalg.vector_norm(a / n - x0) / torch.linalg.vector_norm(x0))
+    batch = dt.Batch([plan])
+
+    def plain():
+        plan.execute(a, b, dt.Execute.FORWARD, aux)
+        plan.execute(b, a, dt.Execute.BACKWARD, aux)
+
+    def graph():
+        batch.execute([a], [b], dt.Execute.FORWARD, [aux], stream)
+        batch.execute([b], [a], dt.Execute.BACKWARD, [aux], stream)
+
+    out = {"workload": "2D C2C complex128 256x256, one process, fwd+bwd", "roundtrip_rel_l2": rt}
+    for name, fn in (("execute", plain), ("graph", graph)):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        k = 200
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        out[name] = {"cycles_per_s": 1000.0 / ms, "ms_per_cycle": ms}
+    out["kernels_per_cycle"] = 2 * 3
+    batch.destroy()
+    plan.destroy()
+    return out
+
+
+def config3_section(args, dt, dev, stream):
+    """3D R2C float64 1024x1024x512 (real input N(0,1)) on a 4x4 virtual grid,
+    and the R2R plan of the same grid with DCT-II on every axis: fwd+bwd
+    cycles/s and the forward error of a spot check against an FP64 DFT of one
+    Z-line (the full FP64 oracle of a 4 GiB transform is the round trip)."""
+    import torch
+    dims = [1024, 1024, 512]
+    comm = dt.cart_comm([1, 4, 4])
+    out = {"dims": dims, "grid": "1x4x4 virtual ranks", "precision": "double"}
+    cfg = dt.Config(stream=stream.cuda_stream)
+    for kind in ("r2c", "r2r_dct2"):
+        if kind == "r2c":
+            plan = dt.PlanR2C(dims, comm=comm, precision=dt.Precision.DOUBLE, executor=dt.Executor.CUFFT, config=cfg)
+            n_in = plan.alloc_size                     # real elements
+            n_out = n_in // 2                          # complex elements
+        else:
+            plan = dt.PlanR2R(dims, kinds=[dt.R2RKind.DCT_2] * 3, comm=comm, precision=dt.Precision.DOUBLE,
+                              executor=dt.Executor.VKFFT, config=cfg)
+            n_in = n_out = plan.alloc_size
+        dt.set_config(dt.Config())
+        g = torch.Generator(device=dev)
+        g.manual_seed(3)
+        x0 = torch.randn(n_in, device=dev, generator=g, dtype=torch.float64)
+        a = x0.clone()
+        b = (torch.empty(n_out, dtype=torch.complex128, device=dev) if kind == "r2c"
+             else torch.empty(n_out, dtype=torch.float64, device=dev))
+        aux = torch.empty_like(b)
+        torch.cuda.synchronize()
+
+        def step():
+            plan.execute(a, b, dt.Execute.FORWARD, aux)
+            plan.execute(b, a, dt.Execute.BACKWARD, aux)
+
+        step()
+        torch.cuda.synchronize()
+        # unnormalised round trip: R2C scales by N, DCT-II/III by prod(2 n)
+        # the real grid is the first prod(dims) elements (an R2C buffer is sized for the complex layouts)
+        nreal = dims[0] * dims[1] * dims[2]
+        scale = float(nreal) * (8.0 if kind != "r2c" else 1.0)
+        rt = float(torch.linalg.vector_norm(a[:nreal] / scale - x0[:nreal]) / torch.linalg.vector_norm(x0[:nreal]))
+        for _ in range(max(1, min(args.warmup, 2))):
+            step()
+        torch.cuda.synchronize()
+        k = 3
+        L = dt.lib()
+        L.dtfft_gb_profile_start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        L.dtfft_gb_profile_stop()
+        ms = e0.elapsed_time(e1) / k
+        prof = sorted(_profile_results(L), key=lambda r: -r[2])
+        out[kind] = {"cycles_per_s": 1000.0 / ms, "ms_per_cycle": ms, "roundtrip_rel_l2": rt,
+                     "kernels": [{"name": r[0], "launches": r[1], "total_ms": r[2]} for r in prof]}
+        plan.destroy()
+        del a, b, aux, x0
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -548,6 +667,11 @@ def run_ours(args):
     if not args.no_tc:
         tensor_core = tensor_core_section(args, dt, dev, stream)
 
+    cfg1 = cfg3 = None
+    if not args.no_configs:
+        cfg1 = config1_section(args, dt, dev, stream)
+        cfg3 = config3_section(args, dt, dev, stream)
+
     batched = None
     if not args.no_batch:
         batched = batched_section(args, dt, dev, stream, peak)
@@ -584,6 +708,8 @@ def run_ours(args):
             "transpose_only": tonly,
             "batched": batched,
             "tensor_core": tensor_core,
+            "config_2d_c128_256x256": cfg1,
+            "config_r2c_f64_1024x1024x512_grid4x4": cfg3,
         }
         print(json.dumps(line), flush=True)
     plan.destroy()
@@ -604,6 +730,8 @@ def main():
     ap.add_argument("--no-transpose-only", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-transform batched section")
     ap.add_argument("--no-tc", action="store_true", help="skip the tensor-core 768^3 / 1024^3 section")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the 2D c128 256x256 and R2C/R2R f64 1024x1024x512 sections")
     ap.add_argument("--dims", type=int, nargs=3, default=None,
                     help="smaller C2C case for profiling (default: the 512^3 headline workload)")
     ap.add_argument("--grid", type=int, nargs=2, default=[2, 4])

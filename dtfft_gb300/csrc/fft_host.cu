@@ -224,15 +224,20 @@ static bool tile_shape(int m, int dbl, bool xpose, TileShape& ts) {
     if (!E || getenv("DTFFT_GB_NO_TILE")) return false;
     const size_t es = dbl ? 16 : 8;
     const size_t cap = max_optin_smem();
+    const size_t hdr = xpose ? kTileHdrXpose : kTileHdrPlain;
     int S = dbl ? 8 : 16;
-    while (S > 2 && 128 + 2 * (size_t)S * m * es > cap) S >>= 1;
+    if (const char* e = getenv("DTFFT_GB_TILE_S")) {   // measurements: rows per tile
+        const int v = atoi(e);
+        if (v >= 2 && v <= S && (v & (v - 1)) == 0) S = v;
+    }
+    while (S > 2 && hdr + 2 * (size_t)S * m * es > cap) S >>= 1;
     const size_t tile = (size_t)S * m * es;
-    const int nst = (int)std::min<size_t>(4, (cap - 128) / tile);
+    const int nst = (int)std::min<size_t>(kTileMaxNst, (cap - hdr) / tile);
     if (nst < 2) return false;
     ts.E = E; ts.S = S; ts.nst = nst;
     ts.threads = dbl ? TilePtr<double>::default_threads(m, xpose) : TilePtr<float>::default_threads(m, xpose);
     if (!xpose) ts.threads = std::min(ts.threads, 32 * S);
-    ts.smem = 128 + (size_t)nst * tile;
+    ts.smem = hdr + (size_t)nst * tile;
     return true;
 }
 

@@ -56,10 +56,16 @@ struct TArgs {
     int ngroups;
     i64 ntiles;
     int S;                // rows per tile (power of two)
-    int nst;              // ring depth (at most 4)
+    int nst;              // ring depth (at most kTileMaxNst)
     int pair_ok;          // xpose, complex64: destinations allow 16-byte stores of two rows
     int* status;
 };
+
+// Ring depth limit and the shared-memory header (mbarriers, flags) in front of
+// the ring: plain kernel kTileHdrPlain bytes, fused kernel kTileHdrXpose.
+constexpr int kTileMaxNst = 8;
+constexpr int kTileHdrPlain = 128;
+constexpr int kTileHdrXpose = 256;
 
 // exchange swizzle (stays inside aligned 16-point blocks; M % 16 == 0)
 __device__ __forceinline__ int xsw(int i) { return i ^ ((i >> 4) & 15); }
@@ -175,7 +181,7 @@ __global__ void __launch_bounds__(32 * NW, 1) fft_tile_kernel(TArgs<R> A) {
     static_assert(M % 16 == 0, "swizzles need 16-point blocks");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
-    C* ring = reinterpret_cast<C*>(smem_raw + 128);
+    C* ring = reinterpret_cast<C*>(smem_raw + kTileHdrPlain);
     const int S = A.S, NST = A.nst;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
 
@@ -257,10 +263,10 @@ __global__ void __launch_bounds__(32 * (NCW + NSW), 1) fft_tile_xpose_kernel(TAr
     // full[b]: the bulk copy into buffer b landed; done[b]: the NCW compute warps
     // wrote its spectra; empty[b]: the NSW store warps have read it
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
-    uint64_t* done = full + 4;
-    uint64_t* empty = full + 8;
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + 96);
-    C* ring = reinterpret_cast<C*>(smem_raw + 128);
+    uint64_t* done = full + kTileMaxNst;
+    uint64_t* empty = full + 2 * kTileMaxNst;
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem_raw + 24 * kTileMaxNst);
+    C* ring = reinterpret_cast<C*>(smem_raw + kTileHdrXpose);
     const int S = A.S, NST = A.nst;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int lgS = __ffs(S) - 1;
