@@ -9,7 +9,7 @@
 #include <sstream>
 
 #include "fft_kernels.cuh"
-#include "fft_tile.cuh"
+#include "fft_rtile.cuh"
 
 namespace gb {
 
@@ -74,6 +74,10 @@ struct FftStep {
     bool tile = false;       // C2C rows: warp-per-row tile kernel (fft_tile.cuh)
     int tile_S = 0, tile_nst = 0, tile_threads = 0, tile_nw = 0;
     size_t tile_smem = 0;
+    bool rt = false;         // C2C rows: runtime-schedule tile kernel (fft_rtile.cuh)
+    int rt_E = 0, rt_T = 0, rt_rpw = 0, rt_S = 0, rt_nst = 0, rt_per_sm = 1;
+    size_t rt_smem = 0;
+    Schedule rt_sched;
     const void* tw_dir = nullptr;   // W_m^(sign*e) for this step's direction
     ~FftStep() { tc_destroy(tc); }
 };
@@ -214,6 +218,47 @@ static dtfft_error_t upload_dir_table(int m, int sign, int dbl, std::vector<void
 
 static size_t max_optin_smem();
 
+// Register schedule of the runtime-schedule tile kernels for rows of m points:
+// T = m / E threads per row (at most 32), every radix dividing E, E one of
+// the compiled counts.  Fewest stages first, then the most lanes busy
+// (rows per warp x T), then the larger E.
+struct RtShape { int E = 0, T = 0, rpw = 0; Schedule sch; };
+static bool rt_schedule(int m, int dbl, RtShape& rs) {
+    // Opt-in (DTFFT_GB_RTILE=1): measured slower than the register / pipelined
+    // kernels on the 7-smooth lengths of the batch workload (e.g. 288^3 C2C:
+    // 2.72 ms vs 1.24 ms per fwd+bwd cycle), so the default path does not use it.
+    const char* on = getenv("DTFFT_GB_RTILE");
+    if (!on || atoi(on) != 1) return false;
+    if (dbl || getenv("DTFFT_GB_NO_TILE")) return false;
+    static const int rads[] = {16, 8, 7, 5, 4, 3, 2};
+    int best_key[3] = {1 << 30, 0, 0};
+    bool found = false;
+    for (int E = 2; E <= 32; ++E) {
+        if (m % E || m / E > 32 || !RtilePtr<float>::has(E)) continue;
+        const int T = m / E;
+        Schedule sc;
+        sc.m = m;
+        int r = m;
+        while (r > 1) {
+            int pick = 0;
+            for (int q : rads)
+                if (E % q == 0 && r % q == 0) { pick = q; break; }
+            if (!pick) break;
+            sc.radix.push_back(pick);
+            r /= pick;
+        }
+        if (r != 1) continue;
+        const int rpw = 32 / T;
+        const int key[3] = {(int)sc.radix.size(), -(rpw * T), -E};
+        if (!found || std::lexicographical_compare(key, key + 3, best_key, best_key + 3)) {
+            found = true;
+            for (int i = 0; i < 3; ++i) best_key[i] = key[i];
+            rs.E = E; rs.T = T; rs.rpw = rpw; rs.sch = sc;
+        }
+    }
+    return found;
+}
+
 // Launch shape of the warp-per-row tile kernel for rows of m points: rows per
 // tile S (one 128-byte run per point when the tile is written transposed),
 // ring depth, threads.  False when no variant is compiled for m or the ring
@@ -337,6 +382,35 @@ static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
             }
         }
     }
+    if (!S.tile && !S.cols && S.mode == M_C2C && S.idist == m && S.odist == m && (m * es) % 16 == 0) {
+        RtShape rs;
+        if (rt_schedule(m, S.dbl, rs)) {
+            // tiles of up to 64 KB; smaller ones (down to 8 KB) while the batch
+            // gives fewer than 8 tiles per SM, so small transforms spread over
+            // several resident CTAs per SM instead of one
+            const size_t row = (size_t)m * es;
+            int rows = 1;
+            while (rows * 2 * row <= 64 * 1024) rows *= 2;
+            while (rows > 1 && (size_t)rows * row > 8 * 1024 && (S.nsig + rows - 1) / rows < (i64)sm_count() * 8)
+                rows /= 2;
+            const size_t tile = (size_t)rows * row;
+            const int nst = 3;
+            const void* fn = RtilePtr<float>::get(rs.E, sign, false);
+            const size_t smem = kTileHdrPlain + (size_t)nst * tile;
+            int per_sm = 0;
+            if (fn && smem <= max_optin_smem() && set_smem_attrs(fn, smem) == DTFFT_SUCCESS &&
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * kRtilePlainWarps, smem) == cudaSuccess &&
+                per_sm > 0) {
+                S.rt = true;
+                S.rt_E = rs.E; S.rt_T = rs.T; S.rt_rpw = rs.rpw; S.rt_S = rows; S.rt_nst = nst;
+                S.rt_smem = smem;
+                S.rt_per_sm = per_sm;
+                S.rt_sched = rs.sch;
+                if (!S.tw_dir) GB_TRY(upload_dir_table(m, sign, S.dbl, owned, &S.tw_dir));
+            }
+            cudaGetLastError();
+        }
+    }
     if (S.E) goto tables;
     {
     const size_t per_sig = 2 * (size_t)m * es;   // ping-pong buffers
@@ -447,6 +521,26 @@ static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, 
         void* tok = prof_begin(s);
         kfn<<<(unsigned)grid, S.tile_threads, S.tile_smem, s>>>(P);
         if (tok) prof_end(tok, std::string("ffttile_rows_c2c_m") + std::to_string(S.m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
+        count_launch();
+        GB_CUDA_TRY(cudaGetLastError());
+        return DTFFT_SUCCESS;
+    }
+    if (!COLS && S.rt && ((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
+        RtArgs<R> P;
+        P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)S.tw_dir;
+        P.M = S.m; P.T = S.rt_T; P.rpw = S.rt_rpw; P.swz = (S.m % 16) == 0;
+        P.st.ns = (int)S.rt_sched.radix.size();
+        for (int i = 0; i < P.st.ns; ++i) P.st.radix[i] = S.rt_sched.radix[i];
+        P.nsig = S.nsig; P.groups = nullptr; P.segs = nullptr; P.ngroups = 0;
+        P.S = S.rt_S; P.K = 1; P.nst = S.rt_nst; P.pair_ok = 0; P.status = status_ptr();
+        P.ntiles = (S.nsig + S.rt_S - 1) / S.rt_S;
+        void (*kfn)(RtArgs<R>) = (void (*)(RtArgs<R>))RtilePtr<R>::get(S.rt_E, S.sign, false);
+        if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+        const i64 grid = std::min<i64>(P.ntiles, (i64)sm_count() * S.rt_per_sm);
+        if (grid <= 0) return DTFFT_SUCCESS;
+        void* tok = prof_begin(s);
+        kfn<<<(unsigned)grid, 32 * kRtilePlainWarps, S.rt_smem, s>>>(P);
+        if (tok) prof_end(tok, std::string("fftrtile_rows_c2c_m") + std::to_string(S.m) + "_f32", s);
         count_launch();
         GB_CUDA_TRY(cudaGetLastError());
         return DTFFT_SUCCESS;
@@ -621,12 +715,23 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
     // warp-per-row tile kernel when one is compiled for m, else the register kernels
     TileShape ts;
     const bool tile = aligned && tile_shape(m, dbl, true, ts);
-    if (tile_only && !tile) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    // runtime-schedule tile kernel for the other lengths with a 32-thread schedule
+    RtShape rs;
+    const bool rt = !tile && aligned && rt_schedule(m, dbl, rs);
+    if (tile_only && !tile && !rt) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     int E = 0, T = 0;
     Schedule sch;
-    int S = 1;
+    int S = 1, K = 1;
     if (tile) {
         S = ts.S;
+    } else if (rt) {
+        // S rows along u (one 128-byte run per point), K slices along w: tiles of
+        // up to 64 KB, fewer slices while the pass gives fewer than 8 tiles per SM
+        S = dbl ? 8 : 16;
+        K = std::max<int>(1, (int)(65536 / ((size_t)S * m * es)));
+        i64 rows = 0;
+        for (const Box& x : bl.host) rows += (i64)x.nb * x.nc;   // upper bound: rows of every box
+        while (K > 1 && rows / ((i64)S * K) < (i64)sm_count() * 8) K = (K + 1) / 2;
     } else {
         if (!make_reg_schedule(m, false, E, sch, T, 64) && !make_reg_schedule(m, false, E, sch, T, 256))
             return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
@@ -664,7 +769,7 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
         segs.insert(segs.end(), gs.begin(), gs.end());
         g.tiles_u = (g.nu + S - 1) / S;
         g.cta_begin = ctas;
-        ctas += (i64)g.tiles_u * g.nw;
+        ctas += (i64)g.tiles_u * ((g.nw + K - 1) / K);
         groups.push_back(g);
         b = e;
     }
@@ -674,7 +779,31 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
     p->ngroups_ = (int)groups.size();
     p->ctas_ = ctas;
     dtfft_error_t err = DTFFT_SUCCESS;
-    if (tile) {
+    if (rt) {
+        const size_t tile_bytes = (size_t)S * K * m * es;
+        const int nst = (int)std::min<size_t>(4, (max_optin_smem() - kTileHdrXpose) / tile_bytes);
+        if (nst < 2) { delete p; return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED; }
+        p->rt_ = true;
+        p->rt_E_ = rs.E; p->rt_T_ = rs.T; p->rt_rpw_ = rs.rpw; p->rt_K_ = K; p->rt_sched_ = rs.sch;
+        p->tile_nst_ = nst;
+        p->smem_ = kTileHdrXpose + (size_t)nst * tile_bytes;
+        int pair = dbl ? 0 : 1;
+        for (const FSeg& sgm : segs) pair = pair && (sgm.dst_off % 2 == 0) && (sgm.di % 2 == 0) && (sgm.dw % 2 == 0);
+        p->pair_ok_ = pair;
+        err = upload_dir_table(m, -1, dbl, p->owned_, &p->tw_);
+        if (err == DTFFT_SUCCESS) err = upload_dir_table(m, 1, dbl, p->owned_, &p->tw_bwd_);
+        for (int sg = -1; sg <= 1 && err == DTFFT_SUCCESS; sg += 2)
+            err = set_smem_attrs(RtilePtr<float>::get(rs.E, sg, true), p->smem_);
+        int per_sm = 0;
+        if (err == DTFFT_SUCCESS &&
+            (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, RtilePtr<float>::get(rs.E, -1, true),
+                                                           32 * (kRtileComputeWarps + kRtileStoreWarps), p->smem_) !=
+                 cudaSuccess ||
+             per_sm < 1))
+            err = DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+        cudaGetLastError();
+        p->rt_per_sm_ = std::max(1, per_sm);
+    } else if (tile) {
         p->tile_ = true;
         p->tile_nst_ = ts.nst;
         p->tile_threads_ = ts.threads;
@@ -726,7 +855,7 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
     if (err == DTFFT_SUCCESS) {
         (void)sm_count();
         (void)status_ptr();
-        if (!tile)
+        if (!tile && !rt)
             err = set_smem_attrs(dbl ? (const void*)KPtr<double>::xpose(E) : (const void*)KPtr<float>::xpose(E),
                                  p->smem_);
     }
@@ -800,6 +929,26 @@ static dtfft_error_t launch_fused_tile(int m, int S, int nst, int threads, int n
 
 dtfft_error_t FusedFT::execute(const void* in, void* out, int sign, cudaStream_t s) {
     if (ctas_ == 0) return DTFFT_SUCCESS;
+    if (rt_) {
+        if (((uintptr_t)in % 16) != 0 || ((uintptr_t)out % 16) != 0) return DTFFT_ERROR_INVALID_USAGE;
+        typedef CT<float>::T C;
+        RtArgs<float> P;
+        P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)(sign > 0 ? tw_bwd_ : tw_);
+        P.M = m_; P.T = rt_T_; P.rpw = rt_rpw_; P.swz = (m_ % 16) == 0;
+        P.st.ns = (int)rt_sched_.radix.size();
+        for (int i = 0; i < P.st.ns; ++i) P.st.radix[i] = rt_sched_.radix[i];
+        P.nsig = 0; P.groups = (const FGroup*)groups_; P.segs = (const FSeg*)segs_; P.ngroups = ngroups_;
+        P.ntiles = ctas_; P.S = S_; P.K = rt_K_; P.nst = tile_nst_; P.pair_ok = pair_ok_; P.status = status_ptr();
+        void (*kfn)(RtArgs<float>) = (void (*)(RtArgs<float>))RtilePtr<float>::get(rt_E_, sign, true);
+        if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+        const i64 grid = std::min<i64>(ctas_, (i64)sm_count() * rt_per_sm_);
+        void* tok = prof_begin(s);
+        kfn<<<(unsigned)grid, 32 * (kRtileComputeWarps + kRtileStoreWarps), smem_, s>>>(P);
+        if (tok) prof_end(tok, std::string("fftrtile_xpose_m") + std::to_string(m_) + "_f32", s);
+        count_launch();
+        GB_CUDA_TRY(cudaGetLastError());
+        return DTFFT_SUCCESS;
+    }
     if (tile_) {
         if (((uintptr_t)in % 16) != 0 || ((uintptr_t)out % 16) != 0) return DTFFT_ERROR_INVALID_USAGE;
         const void* tw = sign > 0 ? tw_bwd_ : tw_;

@@ -220,7 +220,7 @@ static dtfft_error_t build_ffts(Plan& p) {
 // A step that does not fit the fused kernel keeps the two-kernel form.
 static dtfft_error_t build_fused(Plan& p) {
     if (p.transpose_only || p.kind == K_R2R || p.y_slab) return DTFFT_SUCCESS;
-    if (p.z_slab && (p.kind != K_C2C || p.reshape || p.ndims != 3)) return DTFFT_SUCCESS;
+    if (p.z_slab && (p.kind == K_R2R || p.reshape || p.ndims != 3)) return DTFFT_SUCCESS;
     // Default: fuse where the warp-per-row tile kernel takes the rows (it beats
     // FFT + transpose there).  DTFFT_GB_FUSE=1 also fuses the other lengths
     // with the register kernels; DTFFT_GB_FUSE=0 keeps every step unfused.
@@ -242,12 +242,13 @@ static dtfft_error_t build_fused(Plan& p) {
             p.ft[t + 3] = f;
     }
     if (!p.z_slab) return DTFFT_SUCCESS;
-    // A Z-slab C2C plan on one GPU: when all four FFT + transpose passes fuse,
-    // the generic X -> Y -> Z schedule moves the data three times per
-    // direction instead of the slab's four (2D FFT = rows + strided columns,
-    // X -> Z, Z rows), with the same result in the same Z-pencil layout.
-    bool all = true;
-    for (auto st : steps) all = all && p.ft[st.first + 3] != nullptr;
+    // A Z-slab plan on one GPU: when every FFT + transpose pass fuses (C2C: all
+    // four; R2C: the three after the real X axis), the generic X -> Y -> Z
+    // schedule moves the data fewer times than the slab's 2D FFT (rows +
+    // strided columns) + X -> Z + Z rows, with the same result in the same
+    // Z-pencil layout.
+    bool all = true;   // (an R2C plan's X axis is R2C: its step never fuses)
+    for (auto st : steps) all = all && (p.ft[st.first + 3] != nullptr || (p.kind == K_R2C && st.second == 1));
     if (all && build_fft(p, 1, false) == DTFFT_SUCCESS && build_fft(p, 2, false) == DTFFT_SUCCESS) {
         p.zs_generic = true;
         return DTFFT_SUCCESS;

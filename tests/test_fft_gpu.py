@@ -41,6 +41,9 @@ C2C_CASES = [
     ([768, 9, 2], [1, 1, 2], np.complex64),
     ([256, 256, 3], [1, 1, 1], np.complex128),
     ([512, 3, 5], [1, 1, 1], np.complex128),
+    ([48, 320, 288], [1, 1, 1], np.complex64),       # Z-slab plan on the fused generic route
+    ([120, 7, 3], [1, 1, 1], np.complex64),          # runtime-schedule rows, ragged last tile
+    ([50, 90, 13], [1, 2, 1], np.complex64),
 ]
 
 
@@ -83,6 +86,13 @@ def test_c2c_forward_backward(dt, orc, cuda, dims, grid, np_dtype):
     ([512, 40, 12], [1, 3, 1], np.complex128),
     ([256, 512], [1, 2], np.complex64),
     ([512, 256, 32], [1, 1, 1], np.float32),        # R2C: the Y axis (256) fuses
+    # runtime-schedule tile kernels (several rows per warp, K w-slices per tile)
+    ([96, 40, 36], [1, 2, 2], np.complex64),         # M = 96: 4 threads per row, 8 rows per warp
+    ([160, 48, 20], [1, 2, 1], np.complex64),
+    ([384, 36, 10], [1, 3, 1], np.complex64),
+    ([48, 320, 288], [1, 1, 1], np.complex64),       # Z-slab plan on the fused generic route
+    ([100, 96, 160], [1, 1, 1], np.float32),         # R2C Z-slab plan on the fused generic route
+    ([72, 50, 27], [1, 2, 2], np.complex64),         # odd Z (27): that axis stays unfused
 ])
 def test_fused_fft_transpose(dt, orc, cuda, monkeypatch, dims, grid, np_dtype):
     """Plans built with the fused FFT + transpose passes (DTFFT_GB_FUSE=1)."""
@@ -142,6 +152,39 @@ def test_tile_schedules(dt, orc, cuda, dims, grid, np_dtype, inplace):
     plan.destroy()
 
 
+@pytest.mark.parametrize("dims,grid,np_dtype", [
+    ([96, 40, 36], [1, 2, 2], np.complex64),         # M = 96: 4 threads per row, 8 rows per warp
+    ([160, 48, 20], [1, 2, 1], np.complex64),
+    ([384, 36, 10], [1, 3, 1], np.complex64),
+    ([48, 320, 288], [1, 1, 1], np.complex64),       # Z-slab plan on the fused generic route
+    ([100, 96, 160], [1, 1, 1], np.float32),         # R2C Z-slab plan on the fused generic route
+    ([120, 7, 3], [1, 1, 1], np.complex64),          # rows with a ragged last tile
+])
+def test_runtime_tile_kernels(dt, orc, cuda, monkeypatch, dims, grid, np_dtype):
+    """The opt-in runtime-schedule tile kernels (DTFFT_GB_RTILE=1): several rows
+    per warp, run-time radices, K w-slices per fused tile."""
+    monkeypatch.setenv("DTFFT_GB_RTILE", "1")
+    nd = len(dims)
+    if np_dtype == np.float32:
+        plan = dt.PlanR2C(dims, comm=comm_for(dt, grid), precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT)
+        cdt, kind = np.complex64, "r2c"
+    else:
+        plan = dt.PlanC2C(dims, comm=comm_for(dt, grid), precision=_prec(dt, np_dtype), executor=dt.Executor.CUFFT)
+        cdt, kind = np_dtype, "c2c"
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=13)
+    x = orc.global_to_packed(g, nd, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, cdt, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    expect = orc.global_to_packed(orc.forward_values(g, kind), nd, grid, _final_layout(plan, nd))
+    assert orc.rel_l2(from_dev(b, expect.size, cdt), expect) <= TOL[np_dtype]
+    c = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    back = from_dev(c, x.size, np_dtype) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= TOL[np_dtype]
+    plan.destroy()
+
+
 def test_c2c_schedules_agree(dt, orc, cuda):
     """Z-slab, Y-slab and the generic 3-pencil schedule give the same spectrum."""
     dims = [64, 64, 64]
@@ -169,6 +212,8 @@ R2C_CASES = [
     ([64, 32, 36], [1, 4, 4], np.float64),           # 4x4 grid, 33 complex split unevenly
     ([30, 26], [1, 1], np.float32),
     ([21, 16], [1, 2], np.float64),
+    ([100, 96, 160], [1, 1, 1], np.float32),         # Z-slab plan on the fused generic route
+    ([96, 64, 48], [1, 1, 2], np.float32),
 ]
 
 
