@@ -78,14 +78,43 @@ __device__ __forceinline__ int osw(int r, int i, int lgsh) {
     else return i ^ ((r << lgsh) & 7);
 }
 
-template <typename R, int SG, int E, int M, int Ns, int RAD, int... Rest>
+// Radices of a compile-time schedule: first and second stage.
+template <int A, int... Rest>
+struct FirstRad { static constexpr int v = A; };
+template <int A, int B_, int... Rest>
+struct SecondRad { static constexpr int v = B_; };
+
+// Twiddles of the second stage of a warp-row schedule.  When that stage runs
+// one butterfly per thread they depend on the lane only, so a thread loads
+// them once per kernel and keeps them in registers (n > 0); else n = 0 and
+// the stage reads the table.
+template <typename R, int E, int... Rs>
+struct Tw2 {
+    typedef typename CT<R>::T C;
+    static constexpr int R1 = FirstRad<Rs...>::v;
+    static constexpr int R2 = SecondRad<Rs..., 1>::v;
+    static constexpr int M = (Rs * ... * 1);
+    static constexpr int n = (sizeof...(Rs) >= 2 && E == R2 && (M / E) % R1 == 0) ? R2 : 0;
+    C w[n > 0 ? n : 1];
+    __device__ __forceinline__ void load(int t, const C* __restrict__ tw) {
+        if constexpr (n > 0) {
+            const int e1 = (M / (R1 * R2)) * (t % R1);
+#pragma unroll
+            for (int r = 1; r < n; ++r) w[r] = __ldg(&tw[e1 * r]);
+        }
+    }
+};
+
+template <typename R, int SG, int E, int M, int Ns, int NT2, int RAD, int... Rest>
 __device__ __forceinline__ void tile_stages(typename CT<R>::T (&v)[E], int t, const typename CT<R>::T* __restrict__ tw,
-                                            typename CT<R>::T* row) {
+                                            typename CT<R>::T* row, const typename CT<R>::T (&tw2)[NT2]) {
     typedef typename CT<R>::T C;
     constexpr int T = M / E;
     constexpr int B = E / RAD;
     constexpr int tstep = M / (Ns * RAD);
     constexpr bool LAST = sizeof...(Rest) == 0;
+    // second stage with its twiddles in registers (see Tw2)
+    constexpr bool REG_TW = (NT2 == RAD) && (B == 1) && (Ns > 1) && (T % Ns == 0);
 #pragma unroll
     for (int b = 0; b < B; ++b) {
         const int j = t + b * T;
@@ -94,9 +123,14 @@ __device__ __forceinline__ void tile_stages(typename CT<R>::T (&v)[E], int t, co
 #pragma unroll
         for (int r = 0; r < RAD; ++r) w[r] = v[b + r * B];
         if constexpr (Ns > 1) {
-            const int e1 = tstep * k;
+            if constexpr (REG_TW) {
 #pragma unroll
-            for (int r = 1; r < RAD; ++r) w[r] = cmul(w[r], __ldg(&tw[e1 * r]));
+                for (int r = 1; r < RAD; ++r) w[r] = cmul(w[r], tw2[r]);
+            } else {
+                const int e1 = tstep * k;
+#pragma unroll
+                for (int r = 1; r < RAD; ++r) w[r] = cmul(w[r], __ldg(&tw[e1 * r]));
+            }
         }
         dft_any<R, RAD>(w, SG);
         if constexpr (LAST) {
@@ -113,7 +147,14 @@ __device__ __forceinline__ void tile_stages(typename CT<R>::T (&v)[E], int t, co
 #pragma unroll
         for (int q = 0; q < E; ++q) v[q] = row[xsw(t + T * q)];
         __syncwarp();
-        tile_stages<R, SG, E, M, Ns * RAD, Rest...>(v, t, tw, row);
+        // only the second stage may take the register twiddles
+        constexpr int NT2_NEXT = (Ns == 1) ? NT2 : 1;
+        if constexpr (NT2_NEXT == NT2) {
+            tile_stages<R, SG, E, M, Ns * RAD, NT2, Rest...>(v, t, tw, row, tw2);
+        } else {
+            const C none[1] = {tw2[0]};
+            tile_stages<R, SG, E, M, Ns * RAD, 1, Rest...>(v, t, tw, row, none);
+        }
     }
 }
 
@@ -162,12 +203,13 @@ __device__ __forceinline__ void tile_issue(const TArgs<R>& A, i64 tile, typename
 // registers (v[q] = point lane + 32*q).
 template <typename R, int SG, int E, int... Rs>
 __device__ __forceinline__ void tile_row_fft(typename CT<R>::T (&v)[E], typename CT<R>::T* row, int lane,
-                                             const typename CT<R>::T* tw) {
+                                             const typename CT<R>::T* tw, const Tw2<R, E, Rs...>& t2) {
     constexpr int M = (Rs * ... * 1);
+    constexpr int NT2 = Tw2<R, E, Rs...>::n > 0 ? Tw2<R, E, Rs...>::n : 1;
 #pragma unroll
     for (int q = 0; q < E; ++q) v[q] = row[lane + 32 * q];
     __syncwarp();
-    tile_stages<R, SG, E, M, 1, Rs...>(v, lane, tw, row);
+    tile_stages<R, SG, E, M, 1, NT2, Rs...>(v, lane, tw, row, t2.w);
 }
 
 // ---------------------------------------------------------------------------
@@ -184,6 +226,8 @@ __global__ void __launch_bounds__(32 * NW, 1) fft_tile_kernel(TArgs<R> A) {
     C* ring = reinterpret_cast<C*>(smem_raw + kTileHdrPlain);
     const int S = A.S, NST = A.nst;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+    Tw2<R, E, Rs...> t2;
+    t2.load(lane, A.tw);
 
     if (threadIdx.x == 0) {
         for (int b = 0; b < NST; ++b) mbar_init(&bars[b], 1);
@@ -221,7 +265,7 @@ __global__ void __launch_bounds__(32 * NW, 1) fft_tile_kernel(TArgs<R> A) {
         C* tb = ring + (i64)b * S * M;
         for (int rl = warp; rl < nrows; rl += W) {
             C v[E];
-            tile_row_fft<R, SG, E, Rs...>(v, tb + rl * M, lane, A.tw);
+            tile_row_fft<R, SG, E, Rs...>(v, tb + rl * M, lane, A.tw, t2);
             C* dst = A.out + row0 + (i64)rl * M;
 #pragma unroll
             for (int q = 0; q < E; ++q) dst[lane + 32 * q] = v[q];
@@ -286,6 +330,8 @@ __global__ void __launch_bounds__(32 * (NCW + NSW), 1) fft_tile_xpose_kernel(TAr
 
     if (warp < NCW) {
         // ---- compute warps ----
+        Tw2<R, E, Rs...> t2;
+        t2.load(lane, A.tw);
         int b = 0;
         uint32_t par = 0;
         for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
@@ -300,7 +346,7 @@ __global__ void __launch_bounds__(32 * (NCW + NSW), 1) fft_tile_xpose_kernel(TAr
             for (int rl = warp; rl < nrows; rl += NCW) {
                 C* row = tb + rl * M;
                 C v[E];
-                tile_row_fft<R, SG, E, Rs...>(v, row, lane, A.tw);
+                tile_row_fft<R, SG, E, Rs...>(v, row, lane, A.tw, t2);
                 __syncwarp();
 #pragma unroll
                 for (int q = 0; q < E; ++q) row[osw<ES>(rl, lane + 32 * q, lgsh)] = v[q];
