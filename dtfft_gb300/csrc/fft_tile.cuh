@@ -105,9 +105,36 @@ struct Tw2 {
     }
 };
 
-template <typename R, int SG, int E, int M, int Ns, int NT2, int RAD, int... Rest>
+// Twiddles of the last stage: butterfly b of lane t is j = t + 32 b and its
+// twiddles are W^(j r); with at most 8 of them per thread they stay in
+// registers for the whole kernel (n > 0), else the stage reads the table.
+template <int A, int... Rest>
+struct LastRad { static constexpr int v = LastRad<Rest...>::v; };
+template <int A>
+struct LastRad<A> { static constexpr int v = A; };
+
+template <typename R, int E, int... Rs>
+struct Tw3 {
+    typedef typename CT<R>::T C;
+    static constexpr int RL = LastRad<Rs...>::v;
+    static constexpr int B = E / RL;
+    static constexpr int M = (Rs * ... * 1);
+    static constexpr int n = (sizeof...(Rs) >= 2 && M / E == 32 && (RL - 1) * B <= 8) ? (RL - 1) * B : 0;
+    C w[n > 0 ? n : 1];
+    __device__ __forceinline__ void load(int t, const C* __restrict__ tw) {
+        if constexpr (n > 0) {
+#pragma unroll
+            for (int b = 0; b < B; ++b)
+#pragma unroll
+                for (int r = 1; r < RL; ++r) w[b * (RL - 1) + r - 1] = __ldg(&tw[(t + 32 * b) * r]);
+        }
+    }
+};
+
+template <typename R, int SG, int E, int M, int Ns, int NT2, int NT3, int RAD, int... Rest>
 __device__ __forceinline__ void tile_stages(typename CT<R>::T (&v)[E], int t, const typename CT<R>::T* __restrict__ tw,
-                                            typename CT<R>::T* row, const typename CT<R>::T (&tw2)[NT2]) {
+                                            typename CT<R>::T* row, const typename CT<R>::T (&tw2)[NT2],
+                                            const typename CT<R>::T (&tw3)[NT3]) {
     typedef typename CT<R>::T C;
     constexpr int T = M / E;
     constexpr int B = E / RAD;
@@ -115,6 +142,7 @@ __device__ __forceinline__ void tile_stages(typename CT<R>::T (&v)[E], int t, co
     constexpr bool LAST = sizeof...(Rest) == 0;
     // second stage with its twiddles in registers (see Tw2)
     constexpr bool REG_TW = (NT2 == RAD) && (B == 1) && (Ns > 1) && (T % Ns == 0);
+    constexpr bool REG_TW3 = LAST && !REG_TW && (NT3 == (RAD - 1) * B) && (Ns > 1) && (Ns * RAD == M) && (T == 32);
 #pragma unroll
     for (int b = 0; b < B; ++b) {
         const int j = t + b * T;
@@ -126,6 +154,9 @@ __device__ __forceinline__ void tile_stages(typename CT<R>::T (&v)[E], int t, co
             if constexpr (REG_TW) {
 #pragma unroll
                 for (int r = 1; r < RAD; ++r) w[r] = cmul(w[r], tw2[r]);
+            } else if constexpr (REG_TW3) {
+#pragma unroll
+                for (int r = 1; r < RAD; ++r) w[r] = cmul(w[r], tw3[b * (RAD - 1) + r - 1]);
             } else {
                 const int e1 = tstep * k;
 #pragma unroll
@@ -150,10 +181,10 @@ __device__ __forceinline__ void tile_stages(typename CT<R>::T (&v)[E], int t, co
         // only the second stage may take the register twiddles
         constexpr int NT2_NEXT = (Ns == 1) ? NT2 : 1;
         if constexpr (NT2_NEXT == NT2) {
-            tile_stages<R, SG, E, M, Ns * RAD, NT2, Rest...>(v, t, tw, row, tw2);
+            tile_stages<R, SG, E, M, Ns * RAD, NT2, NT3, Rest...>(v, t, tw, row, tw2, tw3);
         } else {
             const C none[1] = {tw2[0]};
-            tile_stages<R, SG, E, M, Ns * RAD, 1, Rest...>(v, t, tw, row, none);
+            tile_stages<R, SG, E, M, Ns * RAD, 1, NT3, Rest...>(v, t, tw, row, none, tw3);
         }
     }
 }
@@ -203,13 +234,15 @@ __device__ __forceinline__ void tile_issue(const TArgs<R>& A, i64 tile, typename
 // registers (v[q] = point lane + 32*q).
 template <typename R, int SG, int E, int... Rs>
 __device__ __forceinline__ void tile_row_fft(typename CT<R>::T (&v)[E], typename CT<R>::T* row, int lane,
-                                             const typename CT<R>::T* tw, const Tw2<R, E, Rs...>& t2) {
+                                             const typename CT<R>::T* tw, const Tw2<R, E, Rs...>& t2,
+                                             const Tw3<R, E, Rs...>& t3) {
     constexpr int M = (Rs * ... * 1);
     constexpr int NT2 = Tw2<R, E, Rs...>::n > 0 ? Tw2<R, E, Rs...>::n : 1;
+    constexpr int NT3 = Tw3<R, E, Rs...>::n > 0 ? Tw3<R, E, Rs...>::n : 1;
 #pragma unroll
     for (int q = 0; q < E; ++q) v[q] = row[lane + 32 * q];
     __syncwarp();
-    tile_stages<R, SG, E, M, 1, NT2, Rs...>(v, lane, tw, row, t2.w);
+    tile_stages<R, SG, E, M, 1, NT2, NT3, Rs...>(v, lane, tw, row, t2.w, t3.w);
 }
 
 // ---------------------------------------------------------------------------
@@ -228,6 +261,8 @@ __global__ void __launch_bounds__(32 * NW, 1) fft_tile_kernel(TArgs<R> A) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     Tw2<R, E, Rs...> t2;
     t2.load(lane, A.tw);
+    Tw3<R, E, Rs...> t3;
+    t3.load(lane, A.tw);
 
     if (threadIdx.x == 0) {
         for (int b = 0; b < NST; ++b) mbar_init(&bars[b], 1);
@@ -265,7 +300,7 @@ __global__ void __launch_bounds__(32 * NW, 1) fft_tile_kernel(TArgs<R> A) {
         C* tb = ring + (i64)b * S * M;
         for (int rl = warp; rl < nrows; rl += W) {
             C v[E];
-            tile_row_fft<R, SG, E, Rs...>(v, tb + rl * M, lane, A.tw, t2);
+            tile_row_fft<R, SG, E, Rs...>(v, tb + rl * M, lane, A.tw, t2, t3);
             C* dst = A.out + row0 + (i64)rl * M;
 #pragma unroll
             for (int q = 0; q < E; ++q) dst[lane + 32 * q] = v[q];
@@ -332,6 +367,8 @@ __global__ void __launch_bounds__(32 * (NCW + NSW), 1) fft_tile_xpose_kernel(TAr
         // ---- compute warps ----
         Tw2<R, E, Rs...> t2;
         t2.load(lane, A.tw);
+        Tw3<R, E, Rs...> t3;
+        t3.load(lane, A.tw);
         int b = 0;
         uint32_t par = 0;
         for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
@@ -346,7 +383,7 @@ __global__ void __launch_bounds__(32 * (NCW + NSW), 1) fft_tile_xpose_kernel(TAr
             for (int rl = warp; rl < nrows; rl += NCW) {
                 C* row = tb + rl * M;
                 C v[E];
-                tile_row_fft<R, SG, E, Rs...>(v, row, lane, A.tw, t2);
+                tile_row_fft<R, SG, E, Rs...>(v, row, lane, A.tw, t2, t3);
                 __syncwarp();
 #pragma unroll
                 for (int q = 0; q < E; ++q) row[osw<ES>(rl, lane + 32 * q, lgsh)] = v[q];
