@@ -84,8 +84,9 @@ struct FirstRad { static constexpr int v = A; };
 template <int A, int B_, int... Rest>
 struct SecondRad { static constexpr int v = B_; };
 
-// Twiddles of the second stage of a warp-row schedule.  When that stage runs
-// one butterfly per thread they depend on the lane only, so a thread loads
+// Twiddles of the second stage of a warp-row schedule.  When the first radix
+// divides the 32 threads of a row, every butterfly of a lane in that stage
+// uses the same twiddles (they depend on the lane only), so a thread loads
 // them once per kernel and keeps them in registers (n > 0); else n = 0 and
 // the stage reads the table.
 template <typename R, int E, int... Rs>
@@ -94,7 +95,7 @@ struct Tw2 {
     static constexpr int R1 = FirstRad<Rs...>::v;
     static constexpr int R2 = SecondRad<Rs..., 1>::v;
     static constexpr int M = (Rs * ... * 1);
-    static constexpr int n = (sizeof...(Rs) >= 2 && E == R2 && (M / E) % R1 == 0) ? R2 : 0;
+    static constexpr int n = (sizeof...(Rs) >= 2 && E % R2 == 0 && (M / E) % R1 == 0) ? R2 : 0;
     C w[n > 0 ? n : 1];
     __device__ __forceinline__ void load(int t, const C* __restrict__ tw) {
         if constexpr (n > 0) {
@@ -141,7 +142,7 @@ __device__ __forceinline__ void tile_stages(typename CT<R>::T (&v)[E], int t, co
     constexpr int tstep = M / (Ns * RAD);
     constexpr bool LAST = sizeof...(Rest) == 0;
     // second stage with its twiddles in registers (see Tw2)
-    constexpr bool REG_TW = (NT2 == RAD) && (B == 1) && (Ns > 1) && (T % Ns == 0);
+    constexpr bool REG_TW = (NT2 == RAD) && (Ns > 1) && (T % Ns == 0);
     constexpr bool REG_TW3 = LAST && !REG_TW && (NT3 == (RAD - 1) * B) && (Ns > 1) && (Ns * RAD == M) && (T == 32);
 #pragma unroll
     for (int b = 0; b < B; ++b) {
