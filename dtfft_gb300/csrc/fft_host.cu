@@ -264,7 +264,12 @@ static bool rt_schedule(int m, int dbl, RtShape& rs) {
 // ring depth, threads.  False when no variant is compiled for m or the ring
 // cannot hold two tiles.
 struct TileShape { int E = 0, S = 0, nst = 0, threads = 0; size_t smem = 0; };
-static bool tile_shape(int m, int dbl, bool xpose, TileShape& ts) {
+static int sm_count();
+
+// rows: rows the launch transforms (0 = unknown).  Tiles shrink (down to 2
+// rows, 1 for complex128 rows without a transpose) while there would be
+// fewer than two per SM, so small transforms still spread over every SM.
+static bool tile_shape(int m, int dbl, bool xpose, TileShape& ts, i64 rows = 0) {
     const int E = dbl ? TilePtr<double>::points_per_thread(m) : TilePtr<float>::points_per_thread(m);
     if (!E || getenv("DTFFT_GB_NO_TILE")) return false;
     const size_t es = dbl ? 16 : 8;
@@ -276,6 +281,8 @@ static bool tile_shape(int m, int dbl, bool xpose, TileShape& ts) {
         if (v >= 2 && v <= S && (v & (v - 1)) == 0) S = v;
     }
     while (S > 2 && hdr + 2 * (size_t)S * m * es > cap) S >>= 1;
+    const int smin = (dbl && !xpose) ? 1 : 2;
+    while (rows > 0 && S > smin && (rows + S - 1) / S < 2 * (i64)sm_count()) S >>= 1;
     const size_t tile = (size_t)S * m * es;
     const int nst = (int)std::min<size_t>(kTileMaxNst, (cap - hdr) / tile);
     if (nst < 2) return false;
@@ -366,7 +373,7 @@ static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
         GB_TRY(tc_create(m, &S.tc));
     if (!S.cols && S.mode == M_C2C && S.idist == m && S.odist == m) {
         TileShape ts;
-        if (tile_shape(m, S.dbl, false, ts)) {
+        if (tile_shape(m, S.dbl, false, ts, S.nsig)) {
             int nw = 0;
             if (const char* tw_env = getenv("DTFFT_GB_TILE_WARPS")) {   // experiments
                 const int w = atoi(tw_env);
@@ -714,7 +721,15 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
                   (x.sc * (i64)es) % 16 == 0;
     // warp-per-row tile kernel when one is compiled for m, else the register kernels
     TileShape ts;
-    const bool tile = aligned && tile_shape(m, dbl, true, ts);
+    i64 box_rows = 0;   // rows of the pass: every box holds nb x nc rows of one source rank
+    {
+        std::vector<std::pair<i64, i64>> seen;
+        for (const Box& x : bl.host) {
+            const std::pair<i64, i64> key(x.src_off - x.a0, (i64)x.nb * x.nc);
+            if (std::find(seen.begin(), seen.end(), key) == seen.end()) { seen.push_back(key); box_rows += key.second; }
+        }
+    }
+    const bool tile = aligned && tile_shape(m, dbl, true, ts, box_rows);
     // runtime-schedule tile kernel for the other lengths with a 32-thread schedule
     RtShape rs;
     const bool rt = !tile && aligned && rt_schedule(m, dbl, rs);
