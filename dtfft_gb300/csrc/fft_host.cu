@@ -938,7 +938,16 @@ static dtfft_error_t launch_fused_tile(int m, int S, int nst, int threads, int n
     kfn<<<(unsigned)grid, threads, smem, s>>>(P);
     if (tok) prof_end(tok, std::string("ffttile_xpose_m") + std::to_string(m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
     count_launch();
-    GB_CUDA_TRY(cudaGetLastError());
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) {
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, (const void*)kfn) == cudaSuccess)
+            fprintf(stderr, "dtFFT-gb300: fused pass m=%d: grid %lld x %d threads, %zu B dynamic smem; kernel: max %d "
+                            "threads, %d registers, max dynamic smem %d B, static smem %zu B\n",
+                    m, (long long)grid, threads, smem, fa.maxThreadsPerBlock, fa.numRegs,
+                    fa.maxDynamicSharedSizeBytes, fa.sharedSizeBytes);
+        GB_CUDA_TRY(le);
+    }
     return DTFFT_SUCCESS;
 }
 

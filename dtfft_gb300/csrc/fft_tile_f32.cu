@@ -31,7 +31,7 @@ void* TilePtr<float>::get(int M, int sign, bool xpose, int ncw, int nsw) {
     }
     switch (M) {
     case 256: GB_XPOSE(3, 5, 8, 8, 8, 4) GB_XPOSE(4, 4, 8, 8, 8, 4) break;
-    case 512: GB_XPOSE(3, 5, 16, 16, 16, 2) GB_XPOSE(4, 4, 16, 16, 16, 2) GB_XPOSE(2, 6, 16, 16, 16, 2) break;
+    case 512: GB_XPOSE(3, 5, 16, 16, 16, 2) GB_XPOSE(4, 4, 16, 16, 16, 2) GB_XPOSE(4, 8, 16, 16, 16, 2) GB_XPOSE(4, 12, 16, 16, 16, 2) GB_XPOSE(6, 6, 16, 16, 16, 2) break;
     case 768: GB_XPOSE(4, 4, 24, 8, 8, 4, 3) GB_XPOSE(3, 5, 24, 8, 8, 4, 3) break;
     case 1024: GB_XPOSE(4, 4, 32, 16, 16, 4) GB_XPOSE(3, 5, 32, 16, 16, 4) break;
     }

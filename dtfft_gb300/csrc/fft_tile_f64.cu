@@ -5,7 +5,9 @@ namespace gb {
 
 template <>
 void* TilePtr<double>::get(int M, int sign, bool xpose, int ncw, int nsw) {
-    (void)ncw; (void)nsw;
+    // one warp split per kind: plain 8 warps, fused 4 compute + 4 store
+    if (!xpose && ncw != 0 && ncw != 8) return nullptr;
+    if (xpose && (ncw != 0 || nsw != 0) && !(ncw == 4 && nsw == 4)) return nullptr;
     if (!xpose) {
         switch (M) {
         case 256: return sign < 0 ? (void*)fft_tile_kernel<double, -1, 8, 8, 8, 8, 4> : (void*)fft_tile_kernel<double, 1, 8, 8, 8, 8, 4>;
