@@ -170,6 +170,8 @@ static bool mode_geometry(int mode, int n, int plan_sign, int& m, int& sign) {
     case M_DCT2: case M_DST2: m = n; sign = -1; break;
     case M_DCT3: case M_DST3: m = n; sign = 1; break;
     case M_DCT4: case M_DST4: m = 2 * n; sign = -1; break;
+    case M_DCT2H: case M_DST2H: m = n / 2; sign = -1; break;
+    case M_DCT3H: case M_DST3H: m = n / 2; sign = 1; break;
     default: return false;
     }
     return m >= 1;
@@ -346,6 +348,15 @@ static dtfft_error_t prepare_launch(const FftStep& S) {
 }
 
 static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
+    // DCT/DST-II and -III of even length through an n/2-point complex FFT when
+    // the register kernel has a schedule for n/2 (half the arithmetic)
+    if ((S.mode == M_DCT2 || S.mode == M_DST2 || S.mode == M_DCT3 || S.mode == M_DST3) && S.n % 2 == 0 &&
+        S.n >= 8 && !getenv("DTFFT_GB_NO_HALF_DCT") && !getenv("DTFFT_GB_NO_REG_FFT")) {
+        int E0 = 0, T0 = 0;
+        Schedule s0;
+        if (make_reg_schedule(S.n / 2, S.cols, E0, s0, T0, 256, S.dbl))
+            S.mode = S.mode == M_DCT2 ? M_DCT2H : S.mode == M_DST2 ? M_DST2H : S.mode == M_DCT3 ? M_DCT3H : M_DST3H;
+    }
     int m, sign;
     if (!mode_geometry(S.mode, S.n, S.sign, m, sign)) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     S.m = m;
@@ -448,6 +459,14 @@ tables:
     case M_C2R_HALF: GB_TRY(upload_table(table_exp(m, 1, S.n), S.dbl, owned, &S.ta)); break;
     case M_DCT2: case M_DST2: case M_DCT3: case M_DST3:
         GB_TRY(upload_table(table_exp(S.n, 1, 4LL * S.n), S.dbl, owned, &S.ta)); break;
+    case M_DCT2H: case M_DST2H:
+        GB_TRY(upload_table(table_exp(m + 1, 1, S.n), S.dbl, owned, &S.ta));
+        GB_TRY(upload_table(table_exp(S.n, 1, 4LL * S.n), S.dbl, owned, &S.tb));
+        break;
+    case M_DCT3H: case M_DST3H:
+        GB_TRY(upload_table(table_exp(m, 1, S.n), S.dbl, owned, &S.ta));
+        GB_TRY(upload_table(table_exp(S.n, 1, 4LL * S.n), S.dbl, owned, &S.tb));
+        break;
     case M_DCT4: case M_DST4: {
         GB_TRY(upload_table(table_exp(S.n, 1, 4LL * S.n), S.dbl, owned, &S.ta));
         std::vector<double> t(2 * (size_t)S.n);
@@ -589,7 +608,7 @@ static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, 
     }
     if (tok) {
         static const char* mn[] = {"c2c", "r2c", "r2c", "c2r", "c2r", "dct1", "dct2", "dct3", "dct4",
-                                   "dst1", "dst2", "dst3", "dst4"};
+                                   "dst1", "dst2", "dst3", "dst4", "dct2h", "dst2h", "dct3h", "dst3h"};
         prof_end(tok, std::string(S.E ? "fftreg_" : "fft_") + (COLS ? "cols_" : "rows_") + mn[S.mode] + "_m" +
                           std::to_string(S.m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
     }

@@ -135,7 +135,10 @@ __device__ __forceinline__ void dft8(C* v, int s) {
 // ---------------------------------------------------------------------------
 enum Mode {
     M_C2C = 0, M_R2C_HALF, M_R2C_FULL, M_C2R_HALF, M_C2R_FULL,
-    M_DCT1, M_DCT2, M_DCT3, M_DCT4, M_DST1, M_DST2, M_DST3, M_DST4
+    M_DCT1, M_DCT2, M_DCT3, M_DCT4, M_DST1, M_DST2, M_DST3, M_DST4,
+    // even n, register kernel only: DCT/DST-II and -III through an n/2-point
+    // complex FFT (the real Makhoul sequence packed two points per complex)
+    M_DCT2H, M_DST2H, M_DCT3H, M_DST3H
 };
 
 struct Stages { int ns; int radix[26]; };
@@ -509,6 +512,21 @@ __device__ __forceinline__ bool reg_stage_any(int rad, typename CT<R>::T (&v)[E]
     return false;
 }
 
+// Makhoul's order of an n-point DCT-II input: v[p] = x[mk_perm(p)]
+__device__ __forceinline__ int mk_perm(int p, int n) { return (2 * p < n) ? 2 * p : 2 * (n - 1 - p) + 1; }
+
+// V[k] = (y[k] - i y[n-k]) conj(W_4n^k) of a DCT-III input (DST-III: y read
+// reversed, y[n-1-k] and y[k-1]); V[0] and V[n/2] are real
+template <typename R, bool COLS>
+__device__ __forceinline__ typename CT<R>::T dct3_v(const Args<R>& A, const R* inR, i64 sig, int k, int n, bool dst) {
+    typedef typename CT<R>::T C;
+    R a, b = 0;
+    if (!dst) { a = inR[gin<R, COLS>(A, sig, k)]; if (k > 0) b = inR[gin<R, COLS>(A, sig, n - k)]; }
+    else { a = inR[gin<R, COLS>(A, sig, n - 1 - k)]; if (k > 0) b = inR[gin<R, COLS>(A, sig, k - 1)]; }
+    C tt; tt.x = a; tt.y = -b;
+    return cmul(tt, cconj(__ldg(&A.tb[k])));
+}
+
 template <typename R, int E, bool COLS, bool C2C_ONLY>
 __global__ void __launch_bounds__(256) fft_reg_kernel(Args<R> A) {
     typedef typename CT<R>::T C;
@@ -575,6 +593,20 @@ __global__ void __launch_bounds__(256) fft_reg_kernel(Args<R> A) {
                     x = cmul(tt, __ldg(&A.ta[i]));
                 }
                 break;
+            case M_DCT2H: case M_DST2H: {   // z[i] = (v[2i], v[2i+1]), DST: odd-indexed x negated
+                const int j0 = mk_perm(2 * i, n), j1 = mk_perm(2 * i + 1, n);
+                R a0 = inR[gin<R, COLS>(A, sig, j0)], a1 = inR[gin<R, COLS>(A, sig, j1)];
+                if (mode == M_DST2H) { if (j0 & 1) a0 = -a0; if (j1 & 1) a1 = -a1; }
+                x.x = a0; x.y = a1;
+            } break;
+            case M_DCT3H: case M_DST3H: {   // half spectrum of the real Makhoul sequence, as C2R
+                C vk = dct3_v<R, COLS>(A, inR, sig, i, n, mode == M_DST3H);
+                C vm = dct3_v<R, COLS>(A, inR, sig, m - i, n, mode == M_DST3H);
+                if (i == 0) { vk.y = 0; vm.y = 0; }
+                C cvm = cconj(vm);
+                C o = cmul(csub(vk, cvm), cconj(__ldg(&A.ta[i])));
+                x = cadd(cadd(vk, cvm), cmul_is(o, 1));
+            } break;
             }
         }
         v[q] = x;
@@ -614,6 +646,30 @@ __global__ void __launch_bounds__(256) fft_reg_kernel(Args<R> A) {
         }
         return;
     }
+    if (mode == M_DCT2H || mode == M_DST2H) {
+        // V[k] (k <= m) of the real Makhoul sequence from Z[k], Z[m-k]; then
+        // y[k] = 2 Re(W_4n^k V[k]) and y[n-k] = 2 Re(W_4n^(n-k) conj(V[k]))
+#pragma unroll
+        for (int q = 0; q < E; ++q) sm[rslot<COLS>(sl, t + T * q, spitch, S)] = v[q];
+        __syncthreads();
+        if (live) {
+            const bool dst = mode == M_DST2H;
+            for (int k = t; k <= m; k += T) {
+                C zk = sm[rslot<COLS>(sl, k == m ? 0 : k, spitch, S)];
+                C zm = cconj(sm[rslot<COLS>(sl, k == 0 ? 0 : m - k, spitch, S)]);
+                C e = cscale(cadd(zk, zm), (R)0.5);
+                C o = cscale(csub(zk, zm), (R)0.5);
+                C V = cadd(e, cmul_is(cmul(__ldg(&A.ta[k]), o), -1));
+                C w = __ldg(&A.tb[k]);
+                outR[gout<R, COLS>(A, sig, dst ? n - 1 - k : k)] = (R)2 * (w.x * V.x - w.y * V.y);
+                if (k > 0 && k < m) {
+                    C w2 = __ldg(&A.tb[n - k]);
+                    outR[gout<R, COLS>(A, sig, dst ? k - 1 : n - k)] = (R)2 * (w2.x * V.x + w2.y * V.y);
+                }
+            }
+        }
+        return;
+    }
     if (!live) return;
 #pragma unroll
     for (int q = 0; q < E; ++q) {
@@ -642,6 +698,13 @@ __global__ void __launch_bounds__(256) fft_reg_kernel(Args<R> A) {
             R y = (R)2 * (w.x * f.x - w.y * f.y);
             if (mode == M_DST4 && (i & 1)) y = -y;
             outR[gout<R, COLS>(A, sig, i)] = y;
+        } break;
+        case M_DCT3H: case M_DST3H: {   // z[i] = (v[2i], v[2i+1]) to Makhoul's positions
+            const int j0 = mk_perm(2 * i, n), j1 = mk_perm(2 * i + 1, n);
+            R a0 = f.x, a1 = f.y;
+            if (mode == M_DST3H) { if (j0 & 1) a0 = -a0; if (j1 & 1) a1 = -a1; }
+            outR[gout<R, COLS>(A, sig, j0)] = a0;
+            outR[gout<R, COLS>(A, sig, j1)] = a1;
         } break;
         }
     }

@@ -269,6 +269,11 @@ def test_r2r_kinds_roundtrip_17x23(dt, orc, cuda, kinds, np_dtype):
     ([16, 12, 20], [1, 2, 2], (5, 4, 6)),
     ([9, 10, 12], [1, 1, 1], (3, 7, 9)),
     ([64, 32, 40], [1, 4, 4], (10, 8, 5)),
+    # even lengths: DCT/DST-II and -III through the n/2-point complex FFT
+    ([16, 24, 32], [1, 1, 1], (9, 9, 9)),
+    ([32, 20, 24], [1, 2, 2], (5, 9, 4)),
+    ([48, 40, 64], [1, 2, 1], (8, 4, 5)),
+    ([8, 10, 12], [1, 1, 1], (4, 8, 9)),
 ])
 def test_r2r_3d(dt, orc, cuda, dims, grid, kinds):
     plan = dt.PlanR2R(dims, kinds=list(kinds), comm=comm_for(dt, grid), precision=dt.Precision.DOUBLE,
@@ -284,6 +289,28 @@ def test_r2r_3d(dt, orc, cuda, dims, grid, kinds):
     plan.execute(b, a, dt.Execute.BACKWARD)
     back = from_dev(a, x.size, np.float64) / orc.r2r_roundtrip_scale(dims, kinds)
     assert np.max(np.abs(back - x)) <= 1e-10
+    plan.destroy()
+
+
+@pytest.mark.parametrize("dims,kinds", [
+    ([40, 24], (5, 9)),        # DCT-II x DST-II, even: n/2-point complex FFTs
+    ([64, 30], (4, 8)),        # DCT-III x DST-III
+    ([24, 96], (9, 4)),
+])
+def test_r2r_even_single(dt, orc, cuda, dims, kinds):
+    """Single-precision R2R kinds on even lengths (half-length FFT path) against
+    the FP64 oracle at the single-precision tolerance."""
+    plan = dt.PlanR2R(dims, kinds=list(kinds), precision=dt.Precision.SINGLE, executor=dt.Executor.VKFFT)
+    g = random_global(tuple(dims[::-1]), np.float32, seed=21, dist="normal")
+    x = orc.global_to_packed(g, 2, [1, 1], 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, np.float32, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    expect = orc.global_to_packed(orc.forward_values(g, "r2r", kinds=list(kinds)), 2, [1, 1], 2)
+    assert orc.rel_l2(from_dev(b, expect.size, np.float32), expect) <= 1e-5
+    plan.execute(b, a, dt.Execute.BACKWARD)
+    back = from_dev(a, x.size, np.float32).astype(np.float64) / orc.r2r_roundtrip_scale(dims, kinds)
+    assert orc.rel_l2(back, x) <= 1e-5
     plan.destroy()
 
 
