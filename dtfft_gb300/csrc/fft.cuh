@@ -83,6 +83,11 @@ public:
     bool usable(const void* in, const void* out) const {
         return !(tile_ || rt_) || (((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0);
     }
+    // Measured choice of the tile kernel's warp split (compute / store warps):
+    // every compiled split is timed with CUDA events on scratch buffers of
+    // max_elems elements and the fastest is kept; choices are cached per
+    // (device, row length, precision, pass geometry) for the process.
+    dtfft_error_t autotune(i64 max_elems, cudaStream_t s, int warmup, int iters, bool log);
 
 private:
     int m_ = 0, dbl_ = 0, E_ = 0, T_ = 0, S_ = 1, pitch_ = 0, ngroups_ = 0;

@@ -970,6 +970,76 @@ static dtfft_error_t launch_fused_tile(int m, int S, int nst, int threads, int n
     return DTFFT_SUCCESS;
 }
 
+// ---------------------------------------------------------------------------
+// Measured warp split of the fused tile pass (part of the EXHAUSTIVE autotune
+// that replaces src/dtfft_nvrtc_block_optimizer.F90's kernel choice)
+// ---------------------------------------------------------------------------
+static std::mutex g_ft_tune_mu;
+static std::map<std::string, std::pair<int, int>> g_ft_tune;
+
+dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int iters, bool log) {
+    if (!tile_ || ctas_ == 0) return DTFFT_SUCCESS;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::ostringstream key;
+    key << dev << "|" << m_ << "|" << dbl_ << "|" << S_ << "|" << ngroups_ << "|" << ctas_ << "|" << smem_;
+    std::lock_guard<std::mutex> lk(g_ft_tune_mu);
+    auto apply = [&](int c, int w) {
+        ncw_ = c; nsw_ = w;
+        const void* f = dbl_ ? TilePtr<double>::get(m_, -1, true, c, w) : TilePtr<float>::get(m_, -1, true, c, w);
+        int threads = 0;
+        if (c == 0) threads = dbl_ ? TilePtr<double>::default_threads(m_, true) : TilePtr<float>::default_threads(m_, true);
+        else threads = 32 * (c + w);
+        tile_threads_ = threads;
+        for (int sg = -1; sg <= 1; sg += 2) {
+            const void* fn = dbl_ ? TilePtr<double>::get(m_, sg, true, c, w) : TilePtr<float>::get(m_, sg, true, c, w);
+            GB_TRY(set_smem_attrs(fn, smem_));
+        }
+        return f ? DTFFT_SUCCESS : DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    };
+    auto it = g_ft_tune.find(key.str());
+    if (it != g_ft_tune.end()) return apply(it->second.first, it->second.second);
+    const size_t bytes = (size_t)max_elems * (dbl_ ? 16 : 8);
+    void *a = nullptr, *b = nullptr;
+    if (cudaMalloc(&a, bytes) != cudaSuccess || cudaMalloc(&b, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        if (a) cudaFree(a);
+        return DTFFT_SUCCESS;   // keep the default split when scratch is not available
+    }
+    cudaMemsetAsync(a, 0, bytes, s);
+    static const int cands[][2] = {{0, 0}, {3, 5}, {4, 4}, {2, 6}, {4, 8}, {6, 6}, {8, 4}};
+    int best_c = 0, best_w = 0;
+    float best_ms = 1e30f;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (const auto& c : cands) {
+        const bool have = c[0] == 0 || (dbl_ ? TilePtr<double>::get(m_, -1, true, c[0], c[1])
+                                             : TilePtr<float>::get(m_, -1, true, c[0], c[1])) != nullptr;
+        if (!have || apply(c[0], c[1]) != DTFFT_SUCCESS) continue;
+        bool ok = true;
+        for (int i = 0; i < warmup && ok; ++i) ok = execute(a, b, -1, s) == DTFFT_SUCCESS;
+        cudaEventRecord(e0, s);
+        for (int i = 0; i < iters && ok; ++i) ok = execute(a, b, -1, s) == DTFFT_SUCCESS;
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        if (!ok) { cudaGetLastError(); continue; }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= (float)std::max(iters, 1);
+        if (log) printf("dtFFT-gb300: fused pass m=%d warps %d+%d: %.4f ms\n", m_, c[0], c[1], ms);
+        if (ms < best_ms) { best_ms = ms; best_c = c[0]; best_w = c[1]; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamSynchronize(s);
+    cudaFree(a);
+    cudaFree(b);
+    cudaGetLastError();
+    g_ft_tune[key.str()] = std::make_pair(best_c, best_w);
+    return apply(best_c, best_w);
+}
+
 dtfft_error_t FusedFT::execute(const void* in, void* out, int sign, cudaStream_t s) {
     if (ctas_ == 0) return DTFFT_SUCCESS;
     if (rt_) {

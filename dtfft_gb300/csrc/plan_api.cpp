@@ -340,6 +340,11 @@ static dtfft_error_t create_plan(int kind, int8_t ndims, const int32_t* dims, co
             e = autotune_boxes(bl, p->alloc_size(), p->stream, cfg.n_measure_warmup_iters, cfg.n_measure_iters, p->log);
             if (e != DTFFT_SUCCESS) break;
         }
+        for (FusedFT* f : p->ft) {
+            if (!f || e != DTFFT_SUCCESS) continue;
+            const i64 elems = p->kind == K_R2C ? p->alloc_size() / 2 : p->alloc_size();   // transformed elements
+            e = f->autotune(elems, p->stream, cfg.n_measure_warmup_iters, cfg.n_measure_iters, p->log);
+        }
     }
     if (e != DTFFT_SUCCESS) { delete p; return e; }
     for (int i = 0; i < ndims; ++i) { p->out_dims[i] = p->dims[i]; p->out_grid[i] = p->grid[i]; }

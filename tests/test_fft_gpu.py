@@ -185,6 +185,30 @@ def test_runtime_tile_kernels(dt, orc, cuda, monkeypatch, dims, grid, np_dtype):
     plan.destroy()
 
 
+@pytest.mark.parametrize("dims,grid,np_dtype", [
+    ([512, 64, 32], [1, 2, 2], np.complex64),
+    ([256, 48, 256], [1, 1, 2], np.complex128),
+])
+def test_exhaustive_tuned_fused_pass(dt, orc, cuda, dims, grid, np_dtype):
+    """EXHAUSTIVE plans time every compiled warp split of the fused tile pass
+    (and the transpose tiles) and keep the fastest; results stay correct."""
+    nd = len(dims)
+    plan = dt.PlanC2C(dims, comm=comm_for(dt, grid), precision=_prec(dt, np_dtype), executor=dt.Executor.CUFFT,
+                      effort=dt.Effort.EXHAUSTIVE)
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=17)
+    x = orc.global_to_packed(g, nd, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    expect = orc.global_to_packed(orc.forward_values(g, "c2c"), nd, grid, _final_layout(plan, nd))
+    assert orc.rel_l2(from_dev(b, expect.size, np_dtype), expect) <= TOL[np_dtype]
+    c = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    back = from_dev(c, x.size, np_dtype).astype(np.complex128) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= TOL[np_dtype]
+    plan.destroy()
+
+
 def test_c2c_schedules_agree(dt, orc, cuda):
     """Z-slab, Y-slab and the generic 3-pencil schedule give the same spectrum."""
     dims = [64, 64, 64]
