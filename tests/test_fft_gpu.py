@@ -409,3 +409,46 @@ def test_device_status_clean_after_runs(dt, cuda):
     torch.cuda.synchronize()
     dt.lib().dtfft_gb_device_status.restype = ctypes.c_int32
     assert dt.lib().dtfft_gb_device_status(0) == 0
+
+
+@pytest.mark.parametrize("dims,grid,np_dtype", [
+    ([1, 16, 12], [1, 1, 1], np.complex64),          # axes of length 1
+    ([16, 1, 12], [1, 1, 1], np.complex64),
+    ([16, 12, 1], [1, 1, 1], np.complex128),
+    ([1, 1, 1], [1, 1, 1], np.complex64),
+    ([4, 1, 6], [1, 2, 2], np.complex64),            # length-1 axis split over ranks (empty ranks)
+    ([2, 3], [1, 1], np.complex128),
+    ([1, 7], [1, 2], np.complex64),
+])
+def test_c2c_degenerate_dims(dt, orc, cuda, dims, grid, np_dtype):
+    nd = len(dims)
+    plan = dt.PlanC2C(dims, comm=comm_for(dt, grid), precision=_prec(dt, np_dtype), executor=dt.Executor.CUFFT)
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=23)
+    x = orc.global_to_packed(g, nd, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    expect = orc.global_to_packed(orc.forward_values(g, "c2c"), nd, grid, _final_layout(plan, nd))
+    assert orc.rel_l2(from_dev(b, expect.size, np_dtype), expect) <= TOL[np_dtype]
+    c = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    back = from_dev(c, x.size, np_dtype).astype(np.complex128) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= TOL[np_dtype]
+    plan.destroy()
+
+
+@pytest.mark.parametrize("dims,kind", [([16, 12, 2], "r2c"), ([2, 8, 6], "r2c"), ([8, 1, 4], "r2c")])
+def test_r2c_degenerate_dims(dt, orc, cuda, dims, kind):
+    plan = dt.PlanR2C(dims, precision=dt.Precision.DOUBLE, executor=dt.Executor.CUFFT)
+    g = random_global(tuple(dims[::-1]), np.float64, seed=29, dist="normal")
+    x = orc.global_to_packed(g, 3, [1, 1, 1], 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size // 2 + 1, np.complex128, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    expect = orc.global_to_packed(orc.forward_values(g, "r2c"), 3, [1, 1, 1], _final_layout(plan, 3))
+    assert orc.rel_l2(from_dev(b, expect.size, np.complex128), expect) <= 1e-12
+    c = empty(plan.alloc_size, np.float64, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    back = from_dev(c, x.size, np.float64) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= 1e-12
+    plan.destroy()
