@@ -50,6 +50,15 @@ dtfft_error_t tc_create(int m, void** out);
 void tc_destroy(void* tc);
 dtfft_error_t tc_execute(void* tc, const void* in, void* out, i64 nsig, int sign, int* status, cudaStream_t s);
 
+// Bluestein form of a batched transform whose length has a prime factor
+// above 127 (fft_bluestein.cu).  kind: 0 C2C, 1 real input (R2C, odd n),
+// 2 Hermitian half input (C2R, odd n).  Geometry as in the kernels' steps:
+// rows signal s at s*idist / s*odist, or columns (cols != 0) of planes.
+dtfft_error_t blue_create(int dbl, int m, int sign, int kind, i64 nsig, i64 idist, i64 odist, i64 plane, int ld,
+                          int ncols, int cols, void** out);
+dtfft_error_t blue_execute(void* b, const void* in, void* out, cudaStream_t s);
+void blue_destroy(void* b);
+
 class FftPlan {
 public:
     static dtfft_error_t create(const FftDesc& d, FftPlan** out);

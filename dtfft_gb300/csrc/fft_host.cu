@@ -71,6 +71,7 @@ struct FftStep {
     int pipe_ctas_per_sm = 0;
     bool reads_out = false;  // step reads the plan's output buffer (second pass)
     void* tc = nullptr;      // tensor-core form of this step (C2C FP32 rows), see fft_tc.cu
+    void* blue = nullptr;    // Bluestein form (a prime factor above 127), see fft_bluestein.cu
     bool tile = false;       // C2C rows: warp-per-row tile kernel (fft_tile.cuh)
     int tile_S = 0, tile_nst = 0, tile_threads = 0, tile_nw = 0;
     size_t tile_smem = 0;
@@ -79,7 +80,7 @@ struct FftStep {
     size_t rt_smem = 0;
     Schedule rt_sched;
     const void* tw_dir = nullptr;   // W_m^(sign*e) for this step's direction
-    ~FftStep() { tc_destroy(tc); }
+    ~FftStep() { tc_destroy(tc); blue_destroy(blue); }
 };
 
 static int g_fft_form = -1;
@@ -378,7 +379,11 @@ static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
             S.pipe = S.pipe_ctas_per_sm > 0;
         }
     } else if (!make_schedule(m, S.sched)) {
-        return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+        // a prime factor above the direct butterflies: Bluestein's chirp-z form
+        const int kind = S.mode == M_C2C ? 0 : S.mode == M_R2C_FULL ? 1 : S.mode == M_C2R_FULL ? 2 : -1;
+        if (kind < 0) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+        return blue_create(S.dbl, m, sign, kind, S.nsig, S.idist, S.odist, S.plane, S.ld, S.ncols, S.cols ? 1 : 0,
+                           &S.blue);
     }
     if (fft_form() == 1 && !S.cols && !S.dbl && S.mode == M_C2C && S.idist == m && S.odist == m && tc_supported(m))
         GB_TRY(tc_create(m, &S.tc));
@@ -524,6 +529,7 @@ static dtfft_error_t launch_pipe(const PArgs<R>& P, int E, int threads, size_t s
 
 template <typename R, bool COLS>
 static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, cudaStream_t s) {
+    if (S.blue) return blue_execute(S.blue, in, out, s);
     if (S.tc) {
         void* tok = prof_begin(s);
         GB_TRY(tc_execute(S.tc, in, out, S.nsig, S.sign, status_ptr(), s));

@@ -452,3 +452,52 @@ def test_r2c_degenerate_dims(dt, orc, cuda, dims, kind):
     back = from_dev(c, x.size, np.float64) / np.prod(dims)
     assert orc.rel_l2(back, x) <= 1e-12
     plan.destroy()
+
+
+@pytest.mark.parametrize("dims,grid,np_dtype", [
+    ([131, 12, 10], [1, 1, 1], np.complex64),        # prime rows above the direct butterflies
+    ([16, 131, 12], [1, 1, 1], np.complex64),        # prime columns of the Z-slab 2D pass
+    ([20, 18, 257], [1, 2, 2], np.complex128),       # prime Z on a 2x2 grid
+    ([262, 9], [1, 1], np.complex64),                # 2 x 131
+    ([139, 130], [1, 2], np.complex128),
+])
+def test_c2c_bluestein_lengths(dt, orc, cuda, dims, grid, np_dtype):
+    """Lengths with a prime factor above 127 take Bluestein's chirp-z form
+    (two power-of-two FFTs per row); the reference's executors accept them too."""
+    nd = len(dims)
+    plan = dt.PlanC2C(dims, comm=comm_for(dt, grid), precision=_prec(dt, np_dtype), executor=dt.Executor.CUFFT)
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=31)
+    x = orc.global_to_packed(g, nd, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    expect = orc.global_to_packed(orc.forward_values(g, "c2c"), nd, grid, _final_layout(plan, nd))
+    assert orc.rel_l2(from_dev(b, expect.size, np_dtype), expect) <= TOL[np_dtype]
+    c = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    back = from_dev(c, x.size, np_dtype).astype(np.complex128) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= TOL[np_dtype]
+    plan.destroy()
+
+
+@pytest.mark.parametrize("dims,grid,np_dtype", [
+    ([131, 12, 10], [1, 1, 1], np.float32),          # odd prime real axis: full-length complex core
+    ([24, 139, 8], [1, 1, 2], np.float64),
+    ([263, 16], [1, 1], np.float64),
+])
+def test_r2c_bluestein_lengths(dt, orc, cuda, dims, grid, np_dtype):
+    nd = len(dims)
+    cdt = np.complex64 if np_dtype == np.float32 else np.complex128
+    plan = dt.PlanR2C(dims, comm=comm_for(dt, grid), precision=_prec(dt, np_dtype), executor=dt.Executor.CUFFT)
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=37, dist="normal")
+    x = orc.global_to_packed(g, nd, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size // 2 + 1, cdt, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    expect = orc.global_to_packed(orc.forward_values(g, "r2c"), nd, grid, _final_layout(plan, nd))
+    assert orc.rel_l2(from_dev(b, expect.size, cdt), expect) <= TOL[np_dtype]
+    c = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    back = from_dev(c, x.size, np_dtype) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= TOL[np_dtype]
+    plan.destroy()
