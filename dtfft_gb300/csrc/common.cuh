@@ -89,10 +89,23 @@ struct BoxList {
     bool copy = false;        // all boxes are copies (a == b)
     int elem = 8;             // element size in bytes
     TransposeConfig cfg;
+    // tensor maps of the TMA transpose per input pointer (transpose_tma.cu)
+    mutable std::vector<std::pair<const void*, void*>> tma_cache;
 };
 
 dtfft_error_t boxes_upload(BoxList& bl);
 void boxes_free(BoxList& bl);
 dtfft_error_t boxes_launch(const BoxList& bl, const void* in, void* out, cudaStream_t stream);
+
+// TMA tensor-load transpose (transpose_tma.cu): boxes it can take, its tile
+// extent along a, the launch, and the release of a list's tensor maps.
+bool tma_eligible(const BoxList& bl);
+int tma_tile_a(int elem);
+dtfft_error_t tma_launch(const BoxList& bl, const void* in, void* out, cudaStream_t s, int* status,
+                         std::vector<std::pair<const void*, void*>>& cache);
+void tma_cache_free(std::vector<std::pair<const void*, void*>>& cache);
+
+// Device status word of the bounded waits (fft_host.cu).
+int* gb_status_word();
 
 }  // namespace gb

@@ -22,6 +22,8 @@ static int* status_ptr() {
     return p;
 }
 
+int* gb_status_word() { return status_ptr(); }
+
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------

@@ -128,6 +128,7 @@ dtfft_error_t boxes_upload(BoxList& bl) {
 void boxes_free(BoxList& bl) {
     if (bl.dev) cudaFree(bl.dev);
     bl.dev = nullptr;
+    tma_cache_free(bl.tma_cache);
 }
 
 template <typename T, int TA, int TB, int ROWS>
@@ -166,6 +167,19 @@ static bool launch_cfg(const BoxList& bl, const void* in, void* out, cudaStream_
 
 dtfft_error_t boxes_launch(const BoxList& bl, const void* in, void* out, cudaStream_t stream) {
     if (bl.total_tiles == 0) return DTFFT_SUCCESS;
+    // TMA tensor loads when the list was tiled for the TMA kernel's extents
+    // (a tensor map the driver refuses to encode leaves the list on the plain kernel)
+    void* tok0 = nullptr;
+    if (!bl.copy && bl.cfg.tile_a == tma_tile_a(bl.elem) && bl.cfg.tile_b == 32 && tma_eligible(bl) &&
+        (tok0 = prof_begin(stream), tma_launch(bl, in, out, stream, gb_status_word(), bl.tma_cache)) == DTFFT_SUCCESS) {
+        void* tok = tok0;
+        if (tok)
+            prof_end(tok, std::string("transpose_tma_e") + std::to_string(bl.elem) + "_t" + std::to_string(bl.cfg.tile_a) +
+                              "x32", stream);
+        count_launch();
+        GB_CUDA_TRY(cudaGetLastError());
+        return DTFFT_SUCCESS;
+    }
     void* tok = prof_begin(stream);
     bool ok = false;
     switch (bl.elem) {
