@@ -442,7 +442,7 @@ const char* dtfft_get_error_string(dtfft_error_t e) {
     case DTFFT_ERROR_INVALID_PLATFORM_EXECUTOR: return "Invalid executor provided for selected platform";
     case DTFFT_ERROR_INVALID_PLATFORM_BACKEND: return "Invalid backend provided for selected platform";
     case DTFFT_ERROR_GPU_CALL_FAILED: return "A CUDA call made by the library failed";
-    case DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED: return "Transform size is not supported by this build's FFT kernels";
+    case DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED: return "Transform size is not supported by this library's FFT kernels";
     case DTFFT_ERROR_NOALLOC_SCRATCH_TOO_SMALL:
         return "Plan needs more scratch than the 16 MiB static buffer of dtfft_execute_noalloc; use dtfft_execute";
     default: return "Unknown error";

@@ -116,7 +116,7 @@ typedef enum {
     DTFFT_ERROR_COMPRESSION_NOT_USED = 506,
     /* Library-specific: a CUDA call failed; the plan stays usable. */
     DTFFT_ERROR_GPU_CALL_FAILED = 600,
-    /* Library-specific: a transform size this build's FFT kernels cannot run. */
+    /* Library-specific: a transform size this library's FFT kernels cannot run. */
     DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED = 601,
     /* Library-specific: the plan needs more scratch than the fixed buffer of
      * dtfft_execute_noalloc holds (dtfft_gb300.h). */

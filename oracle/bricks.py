@@ -1,7 +1,7 @@
 """Oracle (test infrastructure only): decomposition of plans built from
 user-defined blocks, restated in plain Python from the reference.
 
-Only tests/ use this module, as the checker of the library's own geometry
+Only tests/ use this module, as the oracle of the library's own geometry
 (dtfft_vgrid_get_pencil) and data movement.  Parity is pinned by the
 reference's own test of this path, tests/c/test_c2c_3d_c.c:105-136 (2, 4 and 8
 processes on 96x64x512, expected grids 1x1x2, 1x2x2, 1x2x4; in_starts equal

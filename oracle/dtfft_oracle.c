@@ -1,7 +1,7 @@
 /*
  * dtfft_oracle.c -- CPU restatement of dtFFT's data-movement path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU library in
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle of the parity tests of the GPU library in
  * dtfft_gb300/: only tests/, __graft_entry__.smoke() and bench.py's CPU
  * baseline leg may load it.  Nothing in the product links or calls it.
  *

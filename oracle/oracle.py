@@ -1,6 +1,6 @@
 """CPU oracle for dtFFT's single-GPU execute path.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker for the GPU library
+TEST INFRASTRUCTURE ONLY.  This module is the oracle of the GPU library's parity tests
 (`dtfft_gb300`).  Only tests/, __graft_entry__.smoke() and bench.py's
 CPU-baseline leg import it; the product never does.
 
