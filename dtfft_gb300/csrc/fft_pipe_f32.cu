@@ -29,6 +29,19 @@ static void* pipe_ptr(int m, int E) {
     case 20: return (void*)fft_pipe_kernel<float, RtSch<20>, F>;
     case 28: return (void*)fft_pipe_kernel<float, RtSch<28>, F>;
     }
+    // plain rows only: the other points-per-thread counts of the register schedules
+    if (!F) switch (E) {
+    case 7: return (void*)fft_pipe_kernel<float, RtSch<7>, false>;
+    case 9: return (void*)fft_pipe_kernel<float, RtSch<9>, false>;
+    case 10: return (void*)fft_pipe_kernel<float, RtSch<10>, false>;
+    case 12: return (void*)fft_pipe_kernel<float, RtSch<12>, false>;
+    case 14: return (void*)fft_pipe_kernel<float, RtSch<14>, false>;
+    case 15: return (void*)fft_pipe_kernel<float, RtSch<15>, false>;
+    case 18: return (void*)fft_pipe_kernel<float, RtSch<18>, false>;
+    case 21: return (void*)fft_pipe_kernel<float, RtSch<21>, false>;
+    case 25: return (void*)fft_pipe_kernel<float, RtSch<25>, false>;
+    case 30: return (void*)fft_pipe_kernel<float, RtSch<30>, false>;
+    }
     return nullptr;
 }
 
