@@ -501,3 +501,40 @@ def test_r2c_bluestein_lengths(dt, orc, cuda, dims, grid, np_dtype):
     back = from_dev(c, x.size, np_dtype) / np.prod(dims)
     assert orc.rel_l2(back, x) <= TOL[np_dtype]
     plan.destroy()
+
+
+def test_plans_release_device_memory(dt, cuda):
+    """Creating and destroying plans of every kind (fused tile passes, TMA
+    transposes with cached tensor maps, Bluestein scratch, autotuned splits)
+    returns the device memory they took."""
+    import torch
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    free0, _ = torch.cuda.mem_get_info()
+    for it in range(3):
+        plans = [
+            dt.PlanC2C([512, 64, 32], comm=comm_for(dt, [1, 2, 2]), precision=dt.Precision.SINGLE,
+                       executor=dt.Executor.CUFFT, effort=dt.Effort.EXHAUSTIVE),
+            dt.PlanC2C([131, 12, 10], precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT),
+            dt.PlanR2C([64, 32, 36], comm=comm_for(dt, [1, 4, 4]), precision=dt.Precision.DOUBLE,
+                       executor=dt.Executor.CUFFT),
+            dt.PlanR2R([16, 24, 32], kinds=[5, 5, 5], precision=dt.Precision.DOUBLE, executor=dt.Executor.VKFFT),
+        ]
+        for p in plans:
+            n = p.alloc_size
+            a = torch.zeros(n, dtype=torch.float64, device=cuda)
+            b = torch.zeros(n, dtype=torch.float64, device=cuda)
+            torch.cuda.synchronize()
+            if isinstance(p, dt.PlanR2R) or isinstance(p, dt.PlanR2C):
+                p.execute(a, b, dt.Execute.FORWARD)
+            else:
+                p.transpose(a, b, dt.Transpose.X_TO_Y) if p.grid_dims[1] * p.grid_dims[2] > 1 else None
+                p.execute(a, b, dt.Execute.FORWARD)
+            torch.cuda.synchronize()
+            del a, b
+        for p in plans:
+            p.destroy()
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free0 - free1 < 64 << 20, f"{(free0 - free1) >> 20} MiB not returned"
