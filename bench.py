@@ -220,7 +220,7 @@ def batched_section(args, dt, dev, stream, peak):
         for p, (x, o, a) in zip(plain, bufs):
             p.execute(o, x, dt.Execute.BACKWARD, a)
 
-    batch = dt.Batch(tuned, lanes=8)
+    batch = dt.Batch(tuned, lanes=4)
 
     def batch_step():
         batch.execute(ins, outs, dt.Execute.FORWARD, auxs, stream)
