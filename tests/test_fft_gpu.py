@@ -129,6 +129,9 @@ def test_fused_fft_transpose(dt, orc, cuda, monkeypatch, dims, grid, np_dtype):
     ([256, 512, 256], [1, 1, 2], np.complex128, False),  # Z-slab on two virtual ranks
     ([512, 256, 48], [1, 2, 2], np.complex64, True),     # generic schedule, in == out
     ([256, 512], [1, 2], np.complex64, True),            # 2D, in == out
+    ([256, 50, 36], [1, 2, 2], np.complex64, False),     # 25 rows per rank: ragged odd tiles, odd destinations
+    ([512, 50, 36], [1, 2, 2], np.complex128, False),
+    ([768, 24, 20], [1, 2, 1], np.complex64, False),     # store warps write straight from shared memory
 ])
 def test_tile_schedules(dt, orc, cuda, dims, grid, np_dtype, inplace):
     """Fused tile passes on the default path: Z-slab plans take the generic
