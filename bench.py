@@ -42,6 +42,19 @@ def _env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(values, world, device):
+    """Element-wise maximum of per-rank values over all ranks (the slowest
+    rank's time); the values themselves for a single rank."""
+    values = [float(v) for v in values]
+    if world <= 1:
+        return values
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def _peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -557,10 +570,7 @@ def run_ours(args):
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     prof = _profile_results(L)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks([ms], world, dev)[0]
     ms_step = ms / args.steps
     value = world * 1000.0 / ms_step
 
@@ -649,10 +659,7 @@ def run_ours(args):
         lk1.record(s_out)
         torch.cuda.synchronize()
         link_ms = lk0.elapsed_time(lk1) / e2e_steps
-        if world > 1:
-            t = torch.tensor([e2e_ms, link_ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_ms, link_ms = float(t[0].item()), float(t[1].item())
+        e2e_ms, link_ms = max_over_ranks([e2e_ms, link_ms], world, dev)
         del sets
 
     # transpose-only cycle of the same grid (X->Y->Z->Y->X, executor NONE):
