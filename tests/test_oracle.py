@@ -154,3 +154,49 @@ def test_forward_backward_values_roundtrip(orc):
     np.testing.assert_allclose(orc.backward_values(G, "r2c", real_dims=[8, 5, 6]) / g.size, g, atol=1e-12)
     c = g + 1j * rng.standard_normal(g.shape)
     np.testing.assert_allclose(orc.backward_values(orc.forward_values(c, "c2c"), "c2c") / c.size, c, atol=1e-12)
+
+
+def _ramp(n):
+    return np.arange(1, n + 1, dtype=np.float32)
+
+
+@pytest.mark.parametrize("dims", [[33, 77, 21], [90, 57]])
+def test_reference_host_kernel_identities(orc, dims):
+    """The known answers of the reference's host-kernel test
+    (src/tests/test_host_kernels.F90:7-22, :26-236, :287-330) on its dims and
+    ramp input: forward / backward permutes move element (x, y, z) to
+    (y, z, x) / (z, x, y); backward_start followed by backward_end with the
+    neighbour data {nz, nx, ny, 0, 0} equals the one-step backward permute;
+    pack and unpack of a single full block are the identity."""
+    import ctypes
+    L = orc.lib()
+    nd = len(dims)
+    n = int(np.prod(dims))
+    x = _ramp(n)
+    out = np.full(n, -1, dtype=np.float32)
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    dv = (ctypes.c_int * 3)(*(dims + [1] * (3 - nd)))
+    L.orc_permute_forward(ptr(x), ptr(out), nd, dv, 4)
+    if nd == 3:
+        nx, ny, nz = dims
+        g = x.reshape(nz, ny, nx)
+        np.testing.assert_array_equal(out, g.transpose(2, 0, 1).ravel())     # out[x][z][y]
+        back = np.full(n, -1, dtype=np.float32)
+        L.orc_permute_backward(ptr(x), ptr(back), dv, 4)
+        np.testing.assert_array_equal(back, g.transpose(1, 2, 0).ravel())    # out[y][x][z]
+        temp = np.full(n, -1, dtype=np.float32)
+        L.orc_permute_backward_start(ptr(x), ptr(temp), dv, 4)
+        np.testing.assert_array_equal(temp, g.transpose(2, 1, 0).ravel())    # out[x][y][z]
+        tdims = [nz, nx, ny]
+        two = np.full(n, -1, dtype=np.float32)
+        L.orc_permute_backward_end_one(ptr(temp), ptr(two), (ctypes.c_int * 3)(*tdims),
+                                       (ctypes.c_int * 5)(*(tdims + [0, 0])), 4)
+        np.testing.assert_array_equal(two, back)
+    else:
+        nx, ny = dims
+        np.testing.assert_array_equal(out, x.reshape(ny, nx).T.ravel())
+    nb = (ctypes.c_int * 5)(*(dims + [1] * (3 - nd) + [0, 0]))
+    for name in ("orc_unpack_one", "orc_pack_one"):
+        cp = np.full(n, -1, dtype=np.float32)
+        getattr(L, name)(ptr(x), ptr(cp), nd, dv, nb, 4)
+        np.testing.assert_array_equal(cp, x)
