@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdio>
 #include <stdint.h>
@@ -23,6 +24,17 @@ struct __align__(16) e16 { uint64_t lo, hi; };
 // Number of this library's kernel launches since load (benchmark accounting).
 extern std::atomic<int64_t> g_launches;
 inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Host-side trace range (NVTX) around the public entry points, in the places
+// the reference marks with REGION_BEGIN/END (execute, transpose, reshape, plan
+// creation): shown by Nsight tools when one is attached, a few nanoseconds
+// otherwise.
+struct TraceRange {
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 
 // Optional per-launch event timing (profile.cpp); prof_begin returns nullptr when off.
 void* prof_begin(cudaStream_t s);

@@ -264,6 +264,7 @@ static dtfft_error_t build_fused(Plan& p) {
 static dtfft_error_t create_plan(int kind, int8_t ndims, const int32_t* dims, const int32_t* kinds,
                                  MPI_Comm comm, dtfft_precision_t precision, dtfft_effort_t effort,
                                  dtfft_executor_t executor, dtfft_plan_t* out, const UserGeometry* ug = nullptr) {
+    TraceRange tr("dtfft_create_plan");
     if (!out) return DTFFT_ERROR_INVALID_USAGE;
     *out = nullptr;
     // check_create_args order (src/dtfft_plan.F90:2107-2219)
@@ -654,6 +655,7 @@ static dtfft_error_t execute_checks(Plan* p, void* in, void* out, int execute_ty
 }
 
 dtfft_error_t dtfft_execute(dtfft_plan_t plan, void* in, void* out, dtfft_execute_t execute_type, void* aux) {
+    TraceRange tr("dtfft_execute");
     Plan* p = as_plan(plan);
     GB_TRY(execute_checks(p, in, out, (int)execute_type, aux));
     void* a = nullptr;
@@ -669,6 +671,7 @@ namespace gb {
 // the same schedule with `scratch` as aux.  Never allocates.
 dtfft_error_t execute_into_scratch(dtfft_plan_t plan, void* in, void* out, int execute_type, void* scratch,
                                    size_t scratch_bytes, size_t* needed) {
+    TraceRange tr("dtfft_execute_noalloc");
     if (!in || !out) return DTFFT_ERROR_INVALID_USAGE;
     Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
@@ -697,6 +700,7 @@ static dtfft_error_t transpose_checks(Plan* p, void* in, void* out, int t, void*
 }
 
 dtfft_error_t dtfft_transpose(dtfft_plan_t plan, void* in, void* out, dtfft_transpose_t t, void* aux) {
+    TraceRange tr("dtfft_transpose");
     if (!in || !out) return DTFFT_ERROR_INVALID_USAGE;
     Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
@@ -706,6 +710,7 @@ dtfft_error_t dtfft_transpose(dtfft_plan_t plan, void* in, void* out, dtfft_tran
 
 dtfft_error_t dtfft_transpose_start(dtfft_plan_t plan, void* in, void* out, dtfft_transpose_t t, void* aux,
                                     dtfft_request_t* request) {
+    TraceRange tr("dtfft_transpose_start");
     if (!in || !out || !request) return DTFFT_ERROR_INVALID_USAGE;
     Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
@@ -739,6 +744,7 @@ static dtfft_error_t reshape_checks(Plan* p, void* in, void* out, int t, void* a
 }
 
 dtfft_error_t dtfft_reshape(dtfft_plan_t plan, void* in, void* out, dtfft_reshape_t reshape_type, void* aux) {
+    TraceRange tr("dtfft_reshape");
     if (!in || !out) return DTFFT_ERROR_INVALID_USAGE;
     Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
@@ -748,6 +754,7 @@ dtfft_error_t dtfft_reshape(dtfft_plan_t plan, void* in, void* out, dtfft_reshap
 
 dtfft_error_t dtfft_reshape_start(dtfft_plan_t plan, void* in, void* out, dtfft_reshape_t reshape_type, void* aux,
                                   dtfft_request_t* request) {
+    TraceRange tr("dtfft_reshape_start");
     if (!in || !out || !request) return DTFFT_ERROR_INVALID_USAGE;
     Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
@@ -1138,6 +1145,7 @@ dtfft_error_t dtfft_gb_batch_create(int32_t n, const dtfft_plan_t* plans, int32_
 
 dtfft_error_t dtfft_gb_batch_execute(dtfft_gb_batch_t batch, void* const* ins, void* const* outs, void* const* auxs,
                                      dtfft_execute_t execute_type, void* stream) {
+    TraceRange tr("dtfft_gb_batch_execute");
     Batch* b = as_batch(batch);
     if (!b) return DTFFT_ERROR_INVALID_USAGE;
     if (!ins || !outs) return DTFFT_ERROR_INVALID_USAGE;
