@@ -200,3 +200,20 @@ def test_reference_host_kernel_identities(orc, dims):
         cp = np.full(n, -1, dtype=np.float32)
         getattr(L, name)(ptr(x), ptr(cp), nd, dv, nb, 4)
         np.testing.assert_array_equal(cp, x)
+
+
+@pytest.mark.parametrize("dims,grid", [([16, 12, 10], [1, 2, 2]), ([9, 14, 6], [1, 3, 2])])
+def test_cpu_port_computes_the_transform(orc, dims, grid):
+    """The timed CPU baseline (the reference arm of bench.py) runs the real
+    schedule: its forward result is the 3D spectrum in the Z-pencil layout of
+    the grid, and backward(forward(x)) / N returns x."""
+    from oracle import cpu_execute
+    rng = np.random.default_rng(4)
+    g = (rng.uniform(-1, 1, dims[::-1]) + 1j * rng.uniform(-1, 1, dims[::-1])).astype(np.complex64)
+    x = orc.global_to_packed(g, 3, grid, 1)
+    plan = cpu_execute.CpuC2C(dims, grid)
+    y = plan.forward(x)
+    expect = orc.global_to_packed(orc.forward_values(g, "c2c"), 3, grid, 3)
+    assert orc.rel_l2(y[:expect.size], expect) <= 1e-5
+    back = plan.backward(y)[:x.size] / np.prod(dims)
+    assert orc.rel_l2(back, x) <= 1e-5
