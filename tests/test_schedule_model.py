@@ -1,0 +1,84 @@
+"""CPU model of the index arithmetic of the warp-per-row tile kernels
+(dtfft_gb300/csrc/fft_tile.cuh, tile_stages / tile_row_fft): every compiled
+(M, E, radices) schedule, run lane by lane in numpy with the kernels' Stockham
+indices, exchange swizzle and twiddle exponents, must give the DFT of the row
+in natural order (lane t ends with points t + T q).  Also the swizzles the
+kernels rely on are permutations of the row."""
+import numpy as np
+import pytest
+
+# (M, E, radices) of the compiled tile kernels (fft_tile_f32.cu / fft_tile_f64.cu)
+SCHEDULES = [(256, 8, (8, 8, 4)), (512, 16, (16, 16, 2)), (768, 24, (8, 8, 4, 3)), (1024, 32, (16, 16, 4))]
+
+
+def xsw(i):
+    return i ^ ((i >> 4) & 15)
+
+
+def osw8(r, i, lgsh):
+    return i ^ (((r >> 1) << lgsh) & 15)
+
+
+def dft(x, s):
+    n = len(x)
+    k = np.arange(n)
+    return np.exp(s * 2j * np.pi * np.outer(k, k) / n) @ x
+
+
+def model_row(x, E, rads, s):
+    M = len(x)
+    T = M // E
+    tw = np.exp(s * 2j * np.pi * np.arange(M) / M)          # direction table W_M^(s e)
+    row = x.astype(complex).copy()
+    v = np.array([[row[t + T * q] for q in range(E)] for t in range(T)])
+    Ns = 1
+    for si, R in enumerate(rads):
+        last = si == len(rads) - 1
+        B = E // R
+        tstep = M // (Ns * R)
+        new_row = np.full(M, np.nan, dtype=complex)
+        for t in range(T):
+            for b in range(B):
+                j = t + b * T
+                k = (t % Ns) if T % Ns == 0 else (j % Ns)
+                w = np.array([v[t][b + r * B] for r in range(R)])
+                if Ns > 1:
+                    w = w * np.array([tw[(tstep * k * r) % M] for r in range(R)])
+                w = dft(w, s)
+                if last:
+                    for r in range(R):
+                        v[t][b + r * B] = w[r]
+                else:
+                    base = (j - k) * R + k
+                    for r in range(R):
+                        new_row[xsw(base + r * Ns)] = w[r]
+        if not last:
+            assert not np.isnan(new_row).any(), "exchange left a slot unwritten"
+            v = np.array([[new_row[xsw(t + T * q)] for q in range(E)] for t in range(T)])
+        Ns *= R
+    out = np.empty(M, dtype=complex)
+    for t in range(T):
+        for q in range(E):
+            out[t + T * q] = v[t][q]
+    return out
+
+
+@pytest.mark.parametrize("M,E,rads", SCHEDULES)
+@pytest.mark.parametrize("s", [-1, 1])
+def test_tile_schedule_is_the_dft(M, E, rads, s):
+    assert int(np.prod(rads)) == M and M == 32 * E
+    rng = np.random.default_rng(M)
+    x = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    got = model_row(x, E, rads, s)
+    ref = np.fft.fft(x) if s < 0 else np.fft.ifft(x) * M
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-12
+
+
+@pytest.mark.parametrize("M", [256, 512, 768, 1024])
+def test_swizzles_are_permutations(M):
+    assert sorted(xsw(i) for i in range(M)) == list(range(M))
+    for S in (2, 4, 8, 16):                     # complex64 tiles of S rows
+        lgNP = (S.bit_length() - 1) - 1
+        lgsh = 4 - lgNP
+        for r in range(S):
+            assert sorted(osw8(r, i, lgsh) for i in range(M)) == list(range(M))
