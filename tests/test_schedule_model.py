@@ -82,3 +82,42 @@ def test_swizzles_are_permutations(M):
         lgsh = 4 - lgNP
         for r in range(S):
             assert sorted(osw8(r, i, lgsh) for i in range(M)) == list(range(M))
+
+
+def store_warp_writes(M, S, NSW, nrows, segs):
+    """(row, point) pairs each store-warp thread of fft_tile_xpose_kernel
+    writes for one complex64 tile (the loop over segments and points of the
+    kernel's write-out), with the destination element of each."""
+    lgS = S.bit_length() - 1
+    lgNP = lgS - 1
+    gstep = (32 * NSW) >> lgNP
+    out = []
+    for st in range(32 * NSW):
+        lp = st & ((1 << lgNP) - 1)
+        g0 = st >> lgNP
+        for (i0, i1, dst_off, di) in segs:
+            npts = i1 - i0
+            r0 = 2 * lp
+            if r0 >= nrows:
+                continue
+            two = r0 + 1 < nrows
+            for ii in range(g0, npts, gstep):
+                i = i0 + ii
+                d = dst_off + ii * di + r0
+                out.append((r0, i, d))
+                if two:
+                    out.append((r0 + 1, i, d + 1))
+    return out
+
+
+@pytest.mark.parametrize("S", [2, 4, 8, 16])
+@pytest.mark.parametrize("NSW", [4, 5, 8])
+def test_store_warps_write_every_point_once(S, NSW):
+    M = 256
+    segs = [(0, 100, 0, 40), (100, 256, 4000, 40)]      # two destination ranks, 40 rows each
+    for nrows in sorted({1, max(1, S - 1), S}):
+        w = store_warp_writes(M, S, NSW, nrows, segs)
+        assert sorted((r, i) for r, i, _ in w) == [(r, i) for r in range(nrows) for i in range(M)]
+        for r, i, d in w:
+            seg = next(s for s in segs if s[0] <= i < s[1])
+            assert d == seg[2] + (i - seg[0]) * seg[3] + r
