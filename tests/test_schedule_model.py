@@ -121,3 +121,47 @@ def test_store_warps_write_every_point_once(S, NSW):
         for r, i, d in w:
             seg = next(s for s in segs if s[0] <= i < s[1])
             assert d == seg[2] + (i - seg[0]) * seg[3] + r
+
+
+def tma_tile_writes(ES, ra, rb):
+    """(a, b) elements the 256 threads of box_transpose_tma_kernel write for
+    one tile with ra x rb valid elements, and the shared-memory byte offsets
+    they read (transpose_tma.cu)."""
+    IN = 128 // ES
+    TA, TB = 4 * IN, 32
+    writes, reads = [], []
+    for tid in range(256):
+        lane, warp = tid & 31, tid >> 5
+        b = lane
+        if b >= rb:
+            continue
+        if ES == 8:
+            for ap in range(warp, TA // 2, 8):
+                a = 2 * ap
+                if a >= ra:
+                    break
+                k, ai = a // IN, a % IN
+                chunk = ((ai * ES) >> 4) ^ (b & 7)
+                reads.append(k * TB * 128 + b * 128 + chunk * 16)
+                writes.append((a, b))
+                if a + 1 < ra:
+                    writes.append((a + 1, b))
+        else:
+            for a in range(warp, TA, 8):
+                if a >= ra:
+                    break
+                k, ai = a // IN, a % IN
+                chunk = ai ^ (b & 7)
+                reads.append(k * TB * 128 + b * 128 + chunk * 16)
+                writes.append((a, b))
+    return writes, reads, TA, TB
+
+
+@pytest.mark.parametrize("ES", [8, 16])
+def test_tma_transpose_tile_coverage(ES):
+    IN = 128 // ES
+    for ra in sorted({1, 3, IN, 4 * IN - 1, 4 * IN}):
+        for rb in (1, 7, 31, 32):
+            w, r, TA, TB = tma_tile_writes(ES, ra, rb)
+            assert sorted(w) == sorted((a, b) for a in range(ra) for b in range(rb))
+            assert all(0 <= x and x + 16 <= 4 * TB * 128 for x in r)
