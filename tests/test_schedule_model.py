@@ -3,7 +3,10 @@
 (M, E, radices) schedule, run lane by lane in numpy with the kernels' Stockham
 indices, exchange swizzle and twiddle exponents, must give the DFT of the row
 in natural order (lane t ends with points t + T q).  Also the swizzles the
-kernels rely on are permutations of the row."""
+kernels rely on are permutations of the row, the fused kernel's store warps
+write every (row, point) of a tile once to its destination, and the TMA
+transpose writes every element of a tile once with its shared-memory reads
+inside the tile."""
 import numpy as np
 import pytest
 
