@@ -22,6 +22,9 @@ __all__ = [
     "lib", "pencils_comm", "Batch", "DtfftError", "Execute", "Transpose", "Layout", "Reshape", "Precision", "Effort",
     "Executor", "R2RKind", "Backend", "Platform", "Pencil", "Config", "set_config",
     "PlanC2C", "PlanR2C", "PlanR2R", "cart_comm", "world_comm", "COMM_WORLD",
+    "get_backend_string", "get_precision_string", "get_executor_string",
+    "is_fftw_enabled", "is_mkl_enabled", "is_cufft_enabled", "is_vkfft_enabled", "is_cuda_enabled",
+    "is_transpose_only_enabled", "is_nccl_enabled", "is_nvshmem_enabled", "is_compression_enabled",
 ]
 
 _LIB = None
@@ -139,6 +142,62 @@ class Platform(enum.IntEnum):
     CUDA = 2
 
 
+# Build-configuration queries of the reference's Python module
+# (src/interfaces/python/__init__.py: is_*_enabled).  This library is the CUDA
+# platform only; DTFFT_EXECUTOR_CUFFT and DTFFT_EXECUTOR_VKFFT both select its
+# own kernels, and it has no host executors, MPI/NCCL/NVSHMEM backends or
+# compression.
+def is_fftw_enabled() -> bool:
+    return False
+
+
+def is_mkl_enabled() -> bool:
+    return False
+
+
+def is_cufft_enabled() -> bool:
+    return True
+
+
+def is_vkfft_enabled() -> bool:
+    return True
+
+
+def is_cuda_enabled() -> bool:
+    return True
+
+
+def is_transpose_only_enabled() -> bool:
+    return False
+
+
+def is_nccl_enabled() -> bool:
+    return False
+
+
+def is_nvshmem_enabled() -> bool:
+    return False
+
+
+def is_compression_enabled() -> bool:
+    return False
+
+
+def get_backend_string(backend: "Backend") -> str:
+    """Name of a Backend value (dtfft_get_backend_string)."""
+    return lib().dtfft_get_backend_string(int(backend)).decode()
+
+
+def get_precision_string(precision: "Precision") -> str:
+    """Name of a Precision value (dtfft_get_precision_string)."""
+    return lib().dtfft_get_precision_string(int(precision)).decode()
+
+
+def get_executor_string(executor: "Executor") -> str:
+    """Name of an Executor value (dtfft_get_executor_string)."""
+    return lib().dtfft_get_executor_string(int(executor)).decode()
+
+
 class _CPencil(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_uint8), ("ndims", ctypes.c_uint8),
                 ("starts", ctypes.c_int32 * 3), ("counts", ctypes.c_int32 * 3),
@@ -165,6 +224,9 @@ def _declare(L):
     L.dtfft_get_error_string.argtypes = [ctypes.c_int]
     L.dtfft_get_backend_string.restype = ctypes.c_char_p
     L.dtfft_get_backend_string.argtypes = [ctypes.c_int]
+    for name in ("dtfft_get_precision_string", "dtfft_get_executor_string"):
+        getattr(L, name).restype = ctypes.c_char_p
+        getattr(L, name).argtypes = [ctypes.c_int]
     L.dtfft_get_version.restype = i32
     for name in ("dtfft_create_plan_c2c", "dtfft_create_plan_r2c"):
         getattr(L, name).argtypes = [i8, P(i32), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P(vp)]
@@ -402,6 +464,16 @@ class Plan:
     aux_size_reshape = property(lambda s: s._size("dtfft_get_aux_size_reshape"))
     aux_bytes_reshape = property(lambda s: s._size("dtfft_get_aux_bytes_reshape"))
     element_size = property(lambda s: s._size("dtfft_get_element_size"))
+
+    @property
+    def dtype(self):
+        """numpy dtype of the plan's buffers, as the reference's Python Plan
+        derives it: complex for C2C plans, real for R2C and R2R plans."""
+        import numpy as np
+        es = self.element_size
+        if isinstance(self, PlanC2C):
+            return np.dtype(np.complex128 if es == 16 else np.complex64)
+        return np.dtype(np.float64 if es == 8 else np.float32)
 
     @property
     def local_sizes(self):

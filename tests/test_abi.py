@@ -106,3 +106,15 @@ def test_null_handles(dt):
 
 def test_oracle_lib_loads(orc):
     assert orc.lib().orc_num_threads() >= 1
+
+
+def test_module_queries_and_strings(dt):
+    """Module-level queries of the reference's Python module
+    (src/interfaces/python/__init__.py:25-72) and the enum-name strings."""
+    assert dt.is_cuda_enabled() and dt.is_cufft_enabled() and dt.is_vkfft_enabled()
+    assert not (dt.is_fftw_enabled() or dt.is_mkl_enabled() or dt.is_nccl_enabled() or dt.is_nvshmem_enabled()
+                or dt.is_compression_enabled() or dt.is_transpose_only_enabled())
+    names = [dt.get_backend_string(b) for b in dt.Backend]
+    assert all(isinstance(x, str) and x for x in names) and len(set(names)) == len(names)
+    assert dt.get_precision_string(dt.Precision.SINGLE) != dt.get_precision_string(dt.Precision.DOUBLE)
+    assert dt.get_executor_string(dt.Executor.CUFFT)
