@@ -282,12 +282,29 @@ def _declare(L):
     L.dtfft_gb_batch_execute.argtypes = [vp, P(vp), P(vp), P(vp), ctypes.c_int, vp]
     L.dtfft_gb_batch_graph_nodes.argtypes = [vp, P(ctypes.c_int64)]
     L.dtfft_gb_batch_destroy.argtypes = [P(vp)]
-    for name in dir(L):
-        pass
+    L.dtfft_gb_device_status.argtypes = [i32]
+    L.dtfft_gb_device_status.restype = i32
+    L.dtfft_gb_set_wait_limit.argtypes = [i32]
+    L.dtfft_gb_set_wait_limit.restype = i32
 
 
 def kernel_launches() -> int:
     return int(lib().dtfft_gb_kernel_launch_count())
+
+
+def device_status(reset: bool = False) -> int:
+    """Status of the bounded waits on the current device after a device
+    synchronisation (0 = fine; dtfft_gb_device_status)."""
+    return int(lib().dtfft_gb_device_status(1 if reset else 0))
+
+
+def set_wait_limit(iterations: int) -> None:
+    """Iteration limit of the tile kernels' and TMA transpose's waits for their
+    bulk copies (dtfft_gb_set_wait_limit; 0 makes them give up at once)."""
+    _check(lib().dtfft_gb_set_wait_limit(int(iterations)), "dtfft_gb_set_wait_limit")
+
+
+WAIT_LIMIT_DEFAULT = 1 << 22
 
 
 # ---------------------------------------------------------------------------

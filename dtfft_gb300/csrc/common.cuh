@@ -117,7 +117,26 @@ dtfft_error_t tma_launch(const BoxList& bl, const void* in, void* out, cudaStrea
                          std::vector<std::pair<const void*, void*>>& cache);
 void tma_cache_free(std::vector<std::pair<const void*, void*>>& cache);
 
-// Device status word of the bounded waits (fft_host.cu).
+// Status word of the bounded waits on the current device (fft_host.cu): a
+// portable mapped host word per device, created by status_setup() when a
+// plan, kernel or executor is created.  check_device_status() returns
+// DTFFT_ERROR_GPU_WAIT_TIMEOUT (and clears the word) when a kernel on the
+// current device gave up a wait since the last check.
 int* gb_status_word();
+dtfft_error_t status_setup();
+dtfft_error_t check_device_status();
+
+// Iteration limit of the consumer waits of the tile kernels and the TMA
+// transpose (the waits for a bulk copy to land).  The default bounds a wait
+// at well over a second; tests set a limit of 0 through dtfft_gb_set_wait_limit
+// to make a wait run out.  Drains of copies in flight always use the default.
+constexpr int kWaitLimitDefault = 1 << 22;
+extern int g_wait_limit;
+
+// A kernel that gave up a bounded wait records `code` in the status word.
+__device__ __forceinline__ void report_status(int* status, int code) {
+    *reinterpret_cast<volatile int*>(status) = code;
+    __threadfence_system();
+}
 
 }  // namespace gb

@@ -90,7 +90,7 @@ public:
     // False when this pass cannot run on these buffers (the tile kernel's bulk
     // copies need 16-byte aligned rows); the caller then runs FFT + transpose.
     bool usable(const void* in, const void* out) const {
-        return !(tile_ || rt_) || (((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0);
+        return !tile_ || (((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0);
     }
     // Measured choice of the tile kernel's warp split (compute / store warps):
     // every compiled split is timed with CUDA events on scratch buffers of
@@ -108,10 +108,6 @@ private:
     bool tile_ = false;
     int tile_nst_ = 0, tile_threads_ = 0, pair_ok_ = 0, ncw_ = 0, nsw_ = 0;
     const void* tw_bwd_ = nullptr;
-    // runtime-schedule tile kernel (fft_rtile.cuh): used when rt_ is set
-    bool rt_ = false;
-    int rt_E_ = 0, rt_T_ = 0, rt_rpw_ = 0, rt_K_ = 1, rt_per_sm_ = 1;
-    Schedule rt_sched_;
     Schedule sched_;
     const void* tw_ = nullptr;
     const void* groups_ = nullptr;

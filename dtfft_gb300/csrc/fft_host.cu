@@ -4,25 +4,75 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <sstream>
 
 #include "fft_kernels.cuh"
-#include "fft_rtile.cuh"
+#include "fft_tile.cuh"
 
 namespace gb {
 
-// Device status word written by the pipelined kernels when a bounded wait gives up.
-__device__ int g_gb_status = 0;
+// Status words of the bounded waits, one per device, in pinned host memory
+// that every device can write (portable + mapped; with unified addressing the
+// host pointer is also the device pointer on every device).  A kernel whose
+// wait gives up stores its code there; the host reads it without
+// synchronising at the next entry point on that device (check_device_status).
+static constexpr int kStatusDevices = 64;
+static int* g_status = nullptr;
+static dtfft_error_t g_status_err = DTFFT_SUCCESS;
+static std::once_flag g_status_once;
 
+dtfft_error_t status_setup() {
+    std::call_once(g_status_once, [] {
+        void* p = nullptr;
+        if (cudaHostAlloc(&p, sizeof(int) * kStatusDevices, cudaHostAllocPortable | cudaHostAllocMapped) != cudaSuccess) {
+            cudaGetLastError();
+            g_status_err = DTFFT_ERROR_GPU_CALL_FAILED;
+            return;
+        }
+        void* d = nullptr;
+        if (cudaHostGetDevicePointer(&d, p, 0) != cudaSuccess || d != p) {
+            cudaGetLastError();
+            cudaFreeHost(p);
+            g_status_err = DTFFT_ERROR_GPU_CALL_FAILED;
+            return;
+        }
+        memset(p, 0, sizeof(int) * kStatusDevices);
+        g_status = (int*)p;
+    });
+    return g_status_err;
+}
+
+static int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); dev = 0; }
+    return (dev >= 0 && dev < kStatusDevices) ? dev : kStatusDevices - 1;
+}
+
+// Status word of the current device.  Plan, kernel and executor creation call
+// status_setup() first, so a launch never allocates here.
 static int* status_ptr() {
-    static int* p = nullptr;
-    if (!p && cudaGetSymbolAddress((void**)&p, g_gb_status) != cudaSuccess) { cudaGetLastError(); p = nullptr; }
-    return p;
+    if (!g_status && status_setup() != DTFFT_SUCCESS) return nullptr;
+    return g_status + current_device();
 }
 
 int* gb_status_word() { return status_ptr(); }
+
+// Wait limit of the tile kernels' consumer waits (tests shorten it).
+int g_wait_limit = kWaitLimitDefault;
+
+dtfft_error_t check_device_status() {
+    if (!g_status) return DTFFT_SUCCESS;
+    volatile int* w = g_status + current_device();
+    const int v = *w;
+    if (v == 0) return DTFFT_SUCCESS;
+    *w = 0;
+    fprintf(stderr, "dtFFT-gb300: an earlier kernel on this device gave up a bounded wait (code %d); "
+                    "its output was incomplete\n", v);
+    return DTFFT_ERROR_GPU_WAIT_TIMEOUT;
+}
 
 // ---------------------------------------------------------------------------
 // Host side
@@ -77,10 +127,6 @@ struct FftStep {
     bool tile = false;       // C2C rows: warp-per-row tile kernel (fft_tile.cuh)
     int tile_S = 0, tile_nst = 0, tile_threads = 0, tile_nw = 0;
     size_t tile_smem = 0;
-    bool rt = false;         // C2C rows: runtime-schedule tile kernel (fft_rtile.cuh)
-    int rt_E = 0, rt_T = 0, rt_rpw = 0, rt_S = 0, rt_nst = 0, rt_per_sm = 1;
-    size_t rt_smem = 0;
-    Schedule rt_sched;
     const void* tw_dir = nullptr;   // W_m^(sign*e) for this step's direction
     ~FftStep() { tc_destroy(tc); blue_destroy(blue); }
 };
@@ -223,47 +269,6 @@ static dtfft_error_t upload_dir_table(int m, int sign, int dbl, std::vector<void
 
 static size_t max_optin_smem();
 
-// Register schedule of the runtime-schedule tile kernels for rows of m points:
-// T = m / E threads per row (at most 32), every radix dividing E, E one of
-// the compiled counts.  Fewest stages first, then the most lanes busy
-// (rows per warp x T), then the larger E.
-struct RtShape { int E = 0, T = 0, rpw = 0; Schedule sch; };
-static bool rt_schedule(int m, int dbl, RtShape& rs) {
-    // Opt-in (DTFFT_GB_RTILE=1): measured slower than the register / pipelined
-    // kernels on the 7-smooth lengths of the batch workload (e.g. 288^3 C2C:
-    // 2.72 ms vs 1.24 ms per fwd+bwd cycle), so the default path does not use it.
-    const char* on = getenv("DTFFT_GB_RTILE");
-    if (!on || atoi(on) != 1) return false;
-    if (dbl || getenv("DTFFT_GB_NO_TILE")) return false;
-    static const int rads[] = {16, 8, 7, 5, 4, 3, 2};
-    int best_key[3] = {1 << 30, 0, 0};
-    bool found = false;
-    for (int E = 2; E <= 32; ++E) {
-        if (m % E || m / E > 32 || !RtilePtr<float>::has(E)) continue;
-        const int T = m / E;
-        Schedule sc;
-        sc.m = m;
-        int r = m;
-        while (r > 1) {
-            int pick = 0;
-            for (int q : rads)
-                if (E % q == 0 && r % q == 0) { pick = q; break; }
-            if (!pick) break;
-            sc.radix.push_back(pick);
-            r /= pick;
-        }
-        if (r != 1) continue;
-        const int rpw = 32 / T;
-        const int key[3] = {(int)sc.radix.size(), -(rpw * T), -E};
-        if (!found || std::lexicographical_compare(key, key + 3, best_key, best_key + 3)) {
-            found = true;
-            for (int i = 0; i < 3; ++i) best_key[i] = key[i];
-            rs.E = E; rs.T = T; rs.rpw = rpw; rs.sch = sc;
-        }
-    }
-    return found;
-}
-
 // Launch shape of the warp-per-row tile kernel for rows of m points: rows per
 // tile S (one 128-byte run per point when the tile is written transposed),
 // ring depth, threads.  False when no variant is compiled for m or the ring
@@ -342,7 +347,7 @@ static int sm_count();
 
 static dtfft_error_t prepare_launch(const FftStep& S) {
     (void)sm_count();
-    (void)status_ptr();
+    GB_TRY(status_setup());
     const void* fn;
     if (S.E) fn = S.dbl ? (const void*)KPtr<double>::reg(S.E, S.cols, S.mode == M_C2C)
                         : (const void*)KPtr<float>::reg(S.E, S.cols, S.mode == M_C2C);
@@ -405,35 +410,6 @@ static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
                 S.tile_nw = nw;
                 GB_TRY(upload_dir_table(m, sign, S.dbl, owned, &S.tw_dir));
             }
-        }
-    }
-    if (!S.tile && !S.cols && S.mode == M_C2C && S.idist == m && S.odist == m && (m * es) % 16 == 0) {
-        RtShape rs;
-        if (rt_schedule(m, S.dbl, rs)) {
-            // tiles of up to 64 KB; smaller ones (down to 8 KB) while the batch
-            // gives fewer than 8 tiles per SM, so small transforms spread over
-            // several resident CTAs per SM instead of one
-            const size_t row = (size_t)m * es;
-            int rows = 1;
-            while (rows * 2 * row <= 64 * 1024) rows *= 2;
-            while (rows > 1 && (size_t)rows * row > 8 * 1024 && (S.nsig + rows - 1) / rows < (i64)sm_count() * 8)
-                rows /= 2;
-            const size_t tile = (size_t)rows * row;
-            const int nst = 3;
-            const void* fn = RtilePtr<float>::get(rs.E, sign, false);
-            const size_t smem = kTileHdrPlain + (size_t)nst * tile;
-            int per_sm = 0;
-            if (fn && smem <= max_optin_smem() && set_smem_attrs(fn, smem) == DTFFT_SUCCESS &&
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * kRtilePlainWarps, smem) == cudaSuccess &&
-                per_sm > 0) {
-                S.rt = true;
-                S.rt_E = rs.E; S.rt_T = rs.T; S.rt_rpw = rs.rpw; S.rt_S = rows; S.rt_nst = nst;
-                S.rt_smem = smem;
-                S.rt_per_sm = per_sm;
-                S.rt_sched = rs.sch;
-                if (!S.tw_dir) GB_TRY(upload_dir_table(m, sign, S.dbl, owned, &S.tw_dir));
-            }
-            cudaGetLastError();
         }
     }
     if (S.E) goto tables;
@@ -547,7 +523,7 @@ static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, 
         P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)S.tw_dir;
         P.nsig = S.nsig; P.groups = nullptr; P.segs = nullptr; P.ngroups = 0;
         P.ntiles = (S.nsig + S.tile_S - 1) / S.tile_S;
-        P.S = S.tile_S; P.nst = S.tile_nst; P.pair_ok = 0; P.status = status_ptr();
+        P.S = S.tile_S; P.nst = S.tile_nst; P.pair_ok = 0; P.wait_limit = g_wait_limit; P.status = status_ptr();
         void (*kfn)(TArgs<R>) = (void (*)(TArgs<R>))TilePtr<R>::get(S.m, S.sign, false, S.tile_nw);
         if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
         const i64 grid = std::min<i64>(P.ntiles, (i64)sm_count());
@@ -555,26 +531,6 @@ static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, 
         void* tok = prof_begin(s);
         kfn<<<(unsigned)grid, S.tile_threads, S.tile_smem, s>>>(P);
         if (tok) prof_end(tok, std::string("ffttile_rows_c2c_m") + std::to_string(S.m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
-        count_launch();
-        GB_CUDA_TRY(cudaGetLastError());
-        return DTFFT_SUCCESS;
-    }
-    if (!COLS && S.rt && ((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
-        RtArgs<R> P;
-        P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)S.tw_dir;
-        P.M = S.m; P.T = S.rt_T; P.rpw = S.rt_rpw; P.swz = (S.m % 16) == 0;
-        P.st.ns = (int)S.rt_sched.radix.size();
-        for (int i = 0; i < P.st.ns; ++i) P.st.radix[i] = S.rt_sched.radix[i];
-        P.nsig = S.nsig; P.groups = nullptr; P.segs = nullptr; P.ngroups = 0;
-        P.S = S.rt_S; P.K = 1; P.nst = S.rt_nst; P.pair_ok = 0; P.status = status_ptr();
-        P.ntiles = (S.nsig + S.rt_S - 1) / S.rt_S;
-        void (*kfn)(RtArgs<R>) = (void (*)(RtArgs<R>))RtilePtr<R>::get(S.rt_E, S.sign, false);
-        if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-        const i64 grid = std::min<i64>(P.ntiles, (i64)sm_count() * S.rt_per_sm);
-        if (grid <= 0) return DTFFT_SUCCESS;
-        void* tok = prof_begin(s);
-        kfn<<<(unsigned)grid, 32 * kRtilePlainWarps, S.rt_smem, s>>>(P);
-        if (tok) prof_end(tok, std::string("fftrtile_rows_c2c_m") + std::to_string(S.m) + "_f32", s);
         count_launch();
         GB_CUDA_TRY(cudaGetLastError());
         return DTFFT_SUCCESS;
@@ -757,23 +713,12 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
         }
     }
     const bool tile = aligned && tile_shape(m, dbl, true, ts, box_rows);
-    // runtime-schedule tile kernel for the other lengths with a 32-thread schedule
-    RtShape rs;
-    const bool rt = !tile && aligned && rt_schedule(m, dbl, rs);
-    if (tile_only && !tile && !rt) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    if (tile_only && !tile) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     int E = 0, T = 0;
     Schedule sch;
-    int S = 1, K = 1;
+    int S = 1;
     if (tile) {
         S = ts.S;
-    } else if (rt) {
-        // S rows along u (one 128-byte run per point), K slices along w: tiles of
-        // up to 64 KB, fewer slices while the pass gives fewer than 8 tiles per SM
-        S = dbl ? 8 : 16;
-        K = std::max<int>(1, (int)(65536 / ((size_t)S * m * es)));
-        i64 rows = 0;
-        for (const Box& x : bl.host) rows += (i64)x.nb * x.nc;   // upper bound: rows of every box
-        while (K > 1 && rows / ((i64)S * K) < (i64)sm_count() * 8) K = (K + 1) / 2;
     } else {
         if (!make_reg_schedule(m, false, E, sch, T, 64) && !make_reg_schedule(m, false, E, sch, T, 256))
             return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
@@ -811,7 +756,7 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
         segs.insert(segs.end(), gs.begin(), gs.end());
         g.tiles_u = (g.nu + S - 1) / S;
         g.cta_begin = ctas;
-        ctas += (i64)g.tiles_u * ((g.nw + K - 1) / K);
+        ctas += (i64)g.tiles_u * g.nw;
         groups.push_back(g);
         b = e;
     }
@@ -821,31 +766,7 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
     p->ngroups_ = (int)groups.size();
     p->ctas_ = ctas;
     dtfft_error_t err = DTFFT_SUCCESS;
-    if (rt) {
-        const size_t tile_bytes = (size_t)S * K * m * es;
-        const int nst = (int)std::min<size_t>(4, (max_optin_smem() - kTileHdrXpose) / tile_bytes);
-        if (nst < 2) { delete p; return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED; }
-        p->rt_ = true;
-        p->rt_E_ = rs.E; p->rt_T_ = rs.T; p->rt_rpw_ = rs.rpw; p->rt_K_ = K; p->rt_sched_ = rs.sch;
-        p->tile_nst_ = nst;
-        p->smem_ = kTileHdrXpose + (size_t)nst * tile_bytes;
-        int pair = dbl ? 0 : 1;
-        for (const FSeg& sgm : segs) pair = pair && (sgm.dst_off % 2 == 0) && (sgm.di % 2 == 0) && (sgm.dw % 2 == 0);
-        p->pair_ok_ = pair;
-        err = upload_dir_table(m, -1, dbl, p->owned_, &p->tw_);
-        if (err == DTFFT_SUCCESS) err = upload_dir_table(m, 1, dbl, p->owned_, &p->tw_bwd_);
-        for (int sg = -1; sg <= 1 && err == DTFFT_SUCCESS; sg += 2)
-            err = set_smem_attrs(RtilePtr<float>::get(rs.E, sg, true), p->smem_);
-        int per_sm = 0;
-        if (err == DTFFT_SUCCESS &&
-            (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, RtilePtr<float>::get(rs.E, -1, true),
-                                                           32 * (kRtileComputeWarps + kRtileStoreWarps), p->smem_) !=
-                 cudaSuccess ||
-             per_sm < 1))
-            err = DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-        cudaGetLastError();
-        p->rt_per_sm_ = std::max(1, per_sm);
-    } else if (tile) {
+    if (tile) {
         p->tile_ = true;
         p->tile_nst_ = ts.nst;
         p->tile_threads_ = ts.threads;
@@ -896,8 +817,10 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
     }
     if (err == DTFFT_SUCCESS) {
         (void)sm_count();
-        (void)status_ptr();
-        if (!tile && !rt)
+        err = status_setup();
+    }
+    if (err == DTFFT_SUCCESS) {
+        if (!tile)
             err = set_smem_attrs(dbl ? (const void*)KPtr<double>::xpose(E) : (const void*)KPtr<float>::xpose(E),
                                  p->smem_);
     }
@@ -957,7 +880,8 @@ static dtfft_error_t launch_fused_tile(int m, int S, int nst, int threads, int n
     TArgs<R> P;
     P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)tw;
     P.nsig = 0; P.groups = (const FGroup*)groups; P.segs = (const FSeg*)segs; P.ngroups = ngroups;
-    P.ntiles = tiles; P.S = S; P.nst = nst; P.pair_ok = pair_ok; P.status = status_ptr();
+    P.ntiles = tiles; P.S = S; P.nst = nst; P.pair_ok = pair_ok; P.wait_limit = g_wait_limit;
+    P.status = status_ptr();
     void (*kfn)(TArgs<R>) = (void (*)(TArgs<R>))TilePtr<R>::get(m, sign, true, ncw, nsw);
     if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     const i64 grid = std::min<i64>(tiles, (i64)sm_count());
@@ -1050,26 +974,6 @@ dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int i
 
 dtfft_error_t FusedFT::execute(const void* in, void* out, int sign, cudaStream_t s) {
     if (ctas_ == 0) return DTFFT_SUCCESS;
-    if (rt_) {
-        if (((uintptr_t)in % 16) != 0 || ((uintptr_t)out % 16) != 0) return DTFFT_ERROR_INVALID_USAGE;
-        typedef CT<float>::T C;
-        RtArgs<float> P;
-        P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)(sign > 0 ? tw_bwd_ : tw_);
-        P.M = m_; P.T = rt_T_; P.rpw = rt_rpw_; P.swz = (m_ % 16) == 0;
-        P.st.ns = (int)rt_sched_.radix.size();
-        for (int i = 0; i < P.st.ns; ++i) P.st.radix[i] = rt_sched_.radix[i];
-        P.nsig = 0; P.groups = (const FGroup*)groups_; P.segs = (const FSeg*)segs_; P.ngroups = ngroups_;
-        P.ntiles = ctas_; P.S = S_; P.K = rt_K_; P.nst = tile_nst_; P.pair_ok = pair_ok_; P.status = status_ptr();
-        void (*kfn)(RtArgs<float>) = (void (*)(RtArgs<float>))RtilePtr<float>::get(rt_E_, sign, true);
-        if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-        const i64 grid = std::min<i64>(ctas_, (i64)sm_count() * rt_per_sm_);
-        void* tok = prof_begin(s);
-        kfn<<<(unsigned)grid, 32 * (kRtileComputeWarps + kRtileStoreWarps), smem_, s>>>(P);
-        if (tok) prof_end(tok, std::string("fftrtile_xpose_m") + std::to_string(m_) + "_f32", s);
-        count_launch();
-        GB_CUDA_TRY(cudaGetLastError());
-        return DTFFT_SUCCESS;
-    }
     if (tile_) {
         if (((uintptr_t)in % 16) != 0 || ((uintptr_t)out % 16) != 0) return DTFFT_ERROR_INVALID_USAGE;
         const void* tw = sign > 0 ? tw_bwd_ : tw_;
@@ -1096,13 +1000,18 @@ dtfft_error_t FusedFT::execute(const void* in, void* out, int sign, cudaStream_t
 }  // namespace gb
 
 extern "C" int32_t dtfft_gb_device_status(int32_t reset) {
-    int v = -1;
-    if (cudaMemcpyFromSymbol(&v, gb::g_gb_status, sizeof(int)) != cudaSuccess) { cudaGetLastError(); return -1; }
-    if (reset) {
-        int z = 0;
-        cudaMemcpyToSymbol(gb::g_gb_status, &z, sizeof(int));
-    }
+    if (gb::status_setup() != DTFFT_SUCCESS) return -1;
+    if (cudaDeviceSynchronize() != cudaSuccess) { cudaGetLastError(); return -1; }
+    volatile int* w = gb::g_status + gb::current_device();
+    const int v = *w;
+    if (reset) *w = 0;
     return v;
+}
+
+extern "C" int32_t dtfft_gb_set_wait_limit(int32_t iterations) {
+    if (iterations < 0) return DTFFT_ERROR_INVALID_USAGE;
+    gb::g_wait_limit = iterations;
+    return DTFFT_SUCCESS;
 }
 
 extern "C" int32_t dtfft_gb_set_fft_form(int32_t form) {

@@ -854,7 +854,13 @@ __device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* bar, uint32_t parity
 }
 // bounded wait: false after ~2^22 polls (each poll may suspend the thread briefly)
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    for (int it = 0; it < (1 << 22); ++it)
+    for (int it = 0; it < kWaitLimitDefault; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// consumer wait with a launch-time limit (kWaitLimitDefault unless a test shortens it)
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t* bar, uint32_t parity, int limit) {
+    for (int it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -1042,7 +1048,7 @@ __global__ void __launch_bounds__(sizeof(R) == 8 ? 256 : 512) fft_pipe_kernel(PA
         if (__syncthreads_or(!ok)) {
             // give up: record, drain this CTA's copies still in flight, leave
             if (threadIdx.x == 0) {
-                atomicExch(A.status, 1);
+                report_status(A.status, 1);
                 for (int j = 0; j < NST; ++j) {
                     const i64 tj = tile + (i64)j * gridDim.x;
                     if (tj >= A.ntiles) break;

@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
         tc_fence_after();
     }
     if (failed) {
-        if (t == 0) atomicExch(A.status, 2);
+        if (t == 0) report_status(A.status, 2);
         mbar_wait_bounded(bar, phase);   // let the committed MMAs finish before the memory goes away
     }
     tc_fence_before();

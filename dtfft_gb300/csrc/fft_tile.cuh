@@ -58,6 +58,7 @@ struct TArgs {
     int S;                // rows per tile (power of two)
     int nst;              // ring depth (at most kTileMaxNst)
     int pair_ok;          // xpose, complex64: destinations allow 16-byte stores of two rows
+    int wait_limit;       // iteration limit of the waits for a tile's bulk copy
     int* status;
 };
 
@@ -279,10 +280,10 @@ __global__ void __launch_bounds__(32 * NW, 1) fft_tile_kernel(TArgs<R> A) {
     int b = 0;
     uint32_t par = 0;
     for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
-        const bool ok = mbar_wait_bounded(&bars[b], par);
+        const bool ok = mbar_wait_limit(&bars[b], par, A.wait_limit);
         if (__syncthreads_or(!ok)) {
             if (threadIdx.x == 0) {
-                atomicExch(A.status, 1);
+                report_status(A.status, 1);
                 int bb = b;
                 uint32_t pp = par;
                 for (int j = 0; j < NST; ++j) {
@@ -321,8 +322,9 @@ __global__ void __launch_bounds__(32 * NW, 1) fft_tile_kernel(TArgs<R> A) {
 // Rows fused with the transpose (warp-specialised)
 // ---------------------------------------------------------------------------
 // bounded mbarrier wait that also ends when the CTA aborts
-__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
-    for (int it = 0; it < (1 << 22); ++it) {
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                                   int limit = kWaitLimitDefault) {
+    for (int it = 0; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 255) == 255 && *abort_flag) return false;
     }
@@ -373,8 +375,8 @@ __global__ void __launch_bounds__(32 * (NCW + NSW), 1) fft_tile_xpose_kernel(TAr
         int b = 0;
         uint32_t par = 0;
         for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
-            if (!mbar_wait_or_abort(&full[b], par, abort_flag)) {
-                if (lane == 0) { atomicExch(A.status, 1); *abort_flag = 1; }
+            if (!mbar_wait_or_abort(&full[b], par, abort_flag, A.wait_limit)) {
+                if (lane == 0) { report_status(A.status, 1); *abort_flag = 1; }
                 return;
             }
             i64 row0, rs;
@@ -479,7 +481,7 @@ __global__ void __launch_bounds__(32 * (NCW + NSW), 1) fft_tile_xpose_kernel(TAr
         if (++b == NST) { b = 0; par ^= 1; }
     }
     if (failed) {
-        if (lane == 0) { atomicExch(A.status, 1); *abort_flag = 1; }
+        if (lane == 0) { report_status(A.status, 1); *abort_flag = 1; }
         if (producer && lane == 0) {
             // wait (bounded) for the last copy issued into every buffer; a copy
             // that already landed completes its wait at once

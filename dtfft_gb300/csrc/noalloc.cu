@@ -31,22 +31,50 @@ static constexpr size_t kNoAllocScratchBytes = 16u << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 static constexpr int kMaxDevices = 64;
+// Per device: the context the address was looked up in, and the address.
+static void* g_scratch_ctx[kMaxDevices] = {};
 static void* g_scratch_addr[kMaxDevices] = {};
 static std::mutex g_scratch_mu;
 
+typedef int (*CtxGetCurrentFn)(void**);
+static CtxGetCurrentFn g_ctx_get = nullptr;
+static std::once_flag g_ctx_once;
+
+// The current context of the calling thread (the driver's cuCtxGetCurrent,
+// reached through the runtime's entry-point query); nullptr if unavailable.
+static void* current_context() {
+    std::call_once(g_ctx_once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get = (CtxGetCurrentFn)fn;
+        cudaGetLastError();
+    });
+    void* ctx = nullptr;
+    if (!g_ctx_get || g_ctx_get(&ctx) != 0) return nullptr;
+    return ctx;
+}
+
 // Device address of the scratch array on the current device.  The host-side
-// name g_noalloc_scratch is not a device address, so it is looked up once per
-// device with cudaGetSymbolAddress while that device is current.
+// name g_noalloc_scratch is not a device address, so it is looked up with
+// cudaGetSymbolAddress while that device is current: once per device, and
+// again if the device's context has changed since (cudaDeviceReset destroys
+// the context and the module with its array; the next context loads a new
+// copy at another address).
 static dtfft_error_t scratch_address(void** ptr) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return DTFFT_ERROR_GPU_CALL_FAILED; }
     if (dev < 0 || dev >= kMaxDevices) return DTFFT_ERROR_GPU_CALL_FAILED;
     std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
+    void* ctx = current_context();
+    if (!g_scratch_addr[dev] || ctx != g_scratch_ctx[dev]) {
         void* p = nullptr;
         const cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (rc != cudaSuccess || !p) { cudaGetLastError(); return DTFFT_ERROR_GPU_CALL_FAILED; }
         g_scratch_addr[dev] = p;
+        // the lookup may have made the device's primary context current
+        g_scratch_ctx[dev] = current_context();
     }
     *ptr = g_scratch_addr[dev];
     return DTFFT_SUCCESS;

@@ -445,6 +445,8 @@ const char* dtfft_get_error_string(dtfft_error_t e) {
     case DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED: return "Transform size is not supported by this library's FFT kernels";
     case DTFFT_ERROR_NOALLOC_SCRATCH_TOO_SMALL:
         return "Plan needs more scratch than the 16 MiB static buffer of dtfft_execute_noalloc; use dtfft_execute";
+    case DTFFT_ERROR_GPU_WAIT_TIMEOUT:
+        return "A kernel of an earlier call on this device gave up a bounded wait; its output is incomplete";
     default: return "Unknown error";
     }
 }

@@ -331,6 +331,7 @@ static dtfft_error_t create_plan(int kind, int8_t ndims, const int32_t* dims, co
         else if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) == cudaSuccess) p->own_stream = true;
         else e = DTFFT_ERROR_GPU_CALL_FAILED;
     }
+    if (e == DTFFT_SUCCESS) e = status_setup();
     if (e == DTFFT_SUCCESS) e = build_transposes(*p);
     if (e == DTFFT_SUCCESS) e = build_reshapes(*p);
     if (e == DTFFT_SUCCESS) e = build_ffts(*p);
@@ -658,6 +659,7 @@ dtfft_error_t dtfft_execute(dtfft_plan_t plan, void* in, void* out, dtfft_execut
     TraceRange tr("dtfft_execute");
     Plan* p = as_plan(plan);
     GB_TRY(execute_checks(p, in, out, (int)execute_type, aux));
+    GB_TRY(check_device_status());
     void* a = nullptr;
     GB_TRY(get_aux(*p, aux, &a));
     return run_execute(*p, in, out, execute_type == DTFFT_EXECUTE_FORWARD, a, in == out);
@@ -684,6 +686,7 @@ dtfft_error_t execute_into_scratch(dtfft_plan_t plan, void* in, void* out, int e
     if (needed) *needed = p->alloc_bytes();
     if (p->alloc_bytes() > scratch_bytes) return DTFFT_ERROR_NOALLOC_SCRATCH_TOO_SMALL;
     GB_TRY(check_ptrs(in, out, nullptr));
+    GB_TRY(check_device_status());
     return run_execute(*p, in, out, execute_type == DTFFT_EXECUTE_FORWARD, scratch, inplace);
 }
 }  // namespace gb
@@ -705,6 +708,7 @@ dtfft_error_t dtfft_transpose(dtfft_plan_t plan, void* in, void* out, dtfft_tran
     Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
     GB_TRY(transpose_checks(p, in, out, (int)t, aux));
+    GB_TRY(check_device_status());
     return T(*p, (int)t, in, out);
 }
 
@@ -715,6 +719,7 @@ dtfft_error_t dtfft_transpose_start(dtfft_plan_t plan, void* in, void* out, dtff
     Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
     GB_TRY(transpose_checks(p, in, out, (int)t, aux));
+    GB_TRY(check_device_status());
     // the move is one kernel on the plan stream; the request only records it
     GB_TRY(T(*p, (int)t, in, out));
     Request* r = new Request{kReqMagic, (int)t};
@@ -749,6 +754,7 @@ dtfft_error_t dtfft_reshape(dtfft_plan_t plan, void* in, void* out, dtfft_reshap
     Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
     GB_TRY(reshape_checks(p, in, out, (int)reshape_type, aux));
+    GB_TRY(check_device_status());
     return RS(*p, (int)reshape_type, in, out);
 }
 
@@ -759,6 +765,7 @@ dtfft_error_t dtfft_reshape_start(dtfft_plan_t plan, void* in, void* out, dtfft_
     Plan* p = as_plan(plan);
     if (!p) return DTFFT_ERROR_PLAN_NOT_CREATED;
     GB_TRY(reshape_checks(p, in, out, (int)reshape_type, aux));
+    GB_TRY(check_device_status());
     // one copy kernel on the plan stream; the request only records it
     GB_TRY(RS(*p, (int)reshape_type, in, out));
     Request* r = new Request{kReqMagic, (int)reshape_type};
@@ -1149,6 +1156,7 @@ dtfft_error_t dtfft_gb_batch_execute(dtfft_gb_batch_t batch, void* const* ins, v
     Batch* b = as_batch(batch);
     if (!b) return DTFFT_ERROR_INVALID_USAGE;
     if (!ins || !outs) return DTFFT_ERROR_INVALID_USAGE;
+    GB_TRY(check_device_status());
     const int n = (int)b->plans.size();
     std::vector<const void*> key;
     key.reserve(3 * n + 1);

@@ -91,6 +91,7 @@ dtfft_error_t gb_kernel_create(int32_t ndims, const int32_t* dims, int32_t base_
     *kernel = nullptr;
     if (ndims != 2 && ndims != 3) return DTFFT_ERROR_INVALID_N_DIMENSIONS;
     if (base_storage != 4 && base_storage != 8 && base_storage != 16) return DTFFT_ERROR_INVALID_USAGE;
+    GB_TRY(status_setup());
     KernelObj* k = new KernelObj();
     k->type = kernel_type;
     k->ndims = ndims;
@@ -171,6 +172,7 @@ dtfft_error_t gb_kernel_execute(gb_kernel_t kernel, const void* in, void* out, v
     KernelObj* k = reinterpret_cast<KernelObj*>(kernel);
     if (!k || k->magic != 0x4b45524eu) return DTFFT_ERROR_INVALID_USAGE;
     if (k->type == GB_KERNEL_DUMMY) return DTFFT_SUCCESS;
+    GB_TRY(check_device_status());
     cudaStream_t s = (cudaStream_t)stream;
     if (k->type == GB_KERNEL_COPY) {
         size_t n = (size_t)k->dims[0] * k->dims[1] * (k->ndims == 3 ? k->dims[2] : 1);
@@ -212,6 +214,7 @@ dtfft_error_t gb_fft_create(int32_t fft_rank, int32_t fft_type, int32_t precisio
     *fft = nullptr;
     if (fft_rank != 1 && fft_rank != 2) return DTFFT_ERROR_INVALID_USAGE;
     if (precision != DTFFT_SINGLE && precision != DTFFT_DOUBLE) return DTFFT_ERROR_INVALID_PRECISION;
+    GB_TRY(status_setup());
     FftDesc d;
     d.dbl = precision == DTFFT_DOUBLE;
     d.rank = fft_rank;
@@ -244,6 +247,7 @@ dtfft_error_t gb_fft_execute(gb_fft_t fft, void* a, void* b, int32_t sign) {
     FftObj* o = reinterpret_cast<FftObj*>(fft);
     if (!o || o->magic != 0x46465450u) return DTFFT_ERROR_INVALID_USAGE;
     if (sign != GB_FFT_FORWARD && sign != GB_FFT_BACKWARD) return DTFFT_ERROR_INVALID_USAGE;
+    GB_TRY(check_device_status());
     return o->plan->execute(a, b, sign, o->stream);
 }
 

@@ -118,6 +118,7 @@ dtfft_error_t boxes_upload(BoxList& bl) {
     }
     bl.host.swap(kept);
     bl.total_tiles = tiles;
+    GB_TRY(status_setup());
     if (bl.host.empty()) return DTFFT_SUCCESS;
     if (tiles > 0x7fffffffLL) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     GB_CUDA_TRY(cudaMalloc((void**)&bl.dev, sizeof(Box) * bl.host.size()));

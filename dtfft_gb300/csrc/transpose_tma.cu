@@ -32,10 +32,25 @@ struct TmaParams {
     CUtensorMap maps[kTmaMaxBoxes];
     const Box* boxes;
     int nboxes;
+    int wait_limit;
     int* status;
 };
 
 __device__ __forceinline__ uint32_t tma_smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// bounded wait for phase 0 of the tile's mbarrier
+__device__ __forceinline__ bool tma_wait(uint64_t* bar, int limit) {
+    for (int it = 0; it < limit; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(tma_smem_u32(bar))
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
 
 template <int ES>
 __global__ void __launch_bounds__(256) box_transpose_tma_kernel(const __grid_constant__ TmaParams P, char* out) {
@@ -76,18 +91,15 @@ __global__ void __launch_bounds__(256) box_transpose_tma_kernel(const __grid_con
         }
     }
     __syncthreads();
-    bool ok = false;
-    for (int it = 0; it < (1 << 22) && !ok; ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(done)
-            : "r"(tma_smem_u32(&bar))
-            : "memory");
-        ok = done != 0;
-    }
+    bool ok = tma_wait(&bar, P.wait_limit);
     if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) atomicExch(P.status, 3);
+        // give up: record it, and let the loads still in flight land (bounded)
+        // before the CTA's shared memory is released
+        if (threadIdx.x == 0) {
+            report_status(P.status, 3);
+            tma_wait(&bar, kWaitLimitDefault);
+        }
+        __syncthreads();
         return;
     }
     const int ra = min(TA, bx.na - a0), rb = min(TB, bx.nb - b0);
@@ -121,19 +133,19 @@ __global__ void __launch_bounds__(256) box_transpose_tma_kernel(const __grid_con
 // ---------------------------------------------------------------------------
 // host
 // ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode_fn = nullptr;
+static std::once_flag g_encode_once;
+
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    std::call_once(g_encode_once, [] {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+            g_encode_fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
         cudaGetLastError();
-    }
-    return fn;
+    });
+    return g_encode_fn;
 }
 
 // Boxes of this list fit the TMA kernel: 8- or 16-byte elements, at most
@@ -157,8 +169,12 @@ static std::mutex g_tma_mu;
 // input pointer `in` (cached, a few pointers per list).
 dtfft_error_t tma_launch(const BoxList& bl, const void* in, void* out, cudaStream_t s, int* status,
                          std::vector<std::pair<const void*, void*>>& cache) {
-    TmaParams* P = nullptr;
+    // the launch takes a copy made under the lock: another thread may evict
+    // the cached entry as soon as the lock is released
+    if (!status) return DTFFT_ERROR_GPU_CALL_FAILED;
+    TmaParams L;
     {
+        TmaParams* P = nullptr;
         std::lock_guard<std::mutex> lk(g_tma_mu);
         for (auto& e : cache)
             if (e.first == in) P = (TmaParams*)e.second;
@@ -185,12 +201,14 @@ dtfft_error_t tma_launch(const BoxList& bl, const void* in, void* out, cudaStrea
             if (cache.size() >= 4) { delete (TmaParams*)cache.front().second; cache.erase(cache.begin()); }
             cache.emplace_back(in, P);
         }
+        memcpy(&L, P, sizeof(TmaParams));
     }
-    P->status = status;
-    P->boxes = bl.dev;   // re-read: an autotune re-upload may have moved the list
+    L.status = status;
+    L.wait_limit = g_wait_limit;
+    L.boxes = bl.dev;   // re-read: an autotune re-upload may have moved the list
     if (bl.total_tiles == 0) return DTFFT_SUCCESS;
-    if (bl.elem == 8) box_transpose_tma_kernel<8><<<(unsigned)bl.total_tiles, 256, 0, s>>>(*P, (char*)out);
-    else box_transpose_tma_kernel<16><<<(unsigned)bl.total_tiles, 256, 0, s>>>(*P, (char*)out);
+    if (bl.elem == 8) box_transpose_tma_kernel<8><<<(unsigned)bl.total_tiles, 256, 0, s>>>(L, (char*)out);
+    else box_transpose_tma_kernel<16><<<(unsigned)bl.total_tiles, 256, 0, s>>>(L, (char*)out);
     return DTFFT_SUCCESS;
 }
 

@@ -120,7 +120,11 @@ typedef enum {
     DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED = 601,
     /* Library-specific: the plan needs more scratch than the fixed buffer of
      * dtfft_execute_noalloc holds (dtfft_gb300.h). */
-    DTFFT_ERROR_NOALLOC_SCRATCH_TOO_SMALL = 602
+    DTFFT_ERROR_NOALLOC_SCRATCH_TOO_SMALL = 602,
+    /* Library-specific: a kernel launched by an earlier call on this device
+     * gave up a bounded wait and left its output incomplete (reported once,
+     * by the next call on the device; dtfft_gb300.h). */
+    DTFFT_ERROR_GPU_WAIT_TIMEOUT = 603
 } dtfft_error_t;
 
 /** Prints the failing call and aborts (reference: include/dtfft.h:62-70, which calls MPI_Abort). */

@@ -4,9 +4,8 @@
  *
  * 1. Kernel and executor plug-ins.  These are the two seams inside the
  *    reference where its Fortran plan code calls into device code; a
- *    Fortran build of dtFFT binds them with iso_c_binding (INTEGRATION.md
- *    shows the interface blocks) in place of its NVRTC kernels and its cuFFT /
- *    VkFFT executors.
+ *    Fortran build of dtFFT binds them with iso_c_binding interface blocks
+ *    in place of its NVRTC kernels and its cuFFT / VkFFT executors.
  *
  * 2. Virtual-rank queries for plans whose communicator is a grid made by
  *    dtfft_vgrid_cart_create: where each rank's block sits in the one device
@@ -151,8 +150,12 @@ dtfft_error_t dtfft_vgrid_get_pencil(dtfft_plan_t plan, dtfft_layout_t layout, i
  *   DTFFT_ERROR_NOALLOC_SCRATCH_TOO_SMALL.
  * - The first call on a device looks the buffer's device address up
  *   (cudaGetSymbolAddress); make that first call before any stream capture.
- * - Every call on a device shares the one buffer: calls whose kernels overlap
- *   on the GPU (different streams without ordering) race on it.
+ *   The lookup is repeated when the device's context has changed
+ *   (cudaDeviceReset frees the buffer with the context; the next context
+ *   holds a new one).  Plans do not survive a reset: create them again.
+ * - Every call on a device shares the one buffer, which keeps what the last
+ *   call left in it: calls whose kernels overlap on the GPU (different
+ *   streams without ordering) race on it.
  * - Each GPU that loads this code holds the 16 MiB until the process exits.
  */
 dtfft_error_t dtfft_execute_noalloc(dtfft_plan_t plan, void* in, void* out, dtfft_execute_t execute_type);
@@ -212,12 +215,30 @@ int32_t dtfft_gb_get_fft_form(void);
 int64_t dtfft_gb_kernel_launch_count(void);
 
 /**
- * Device-side status word of the pipelined kernels: 0 = fine, 1 = a bounded
- * wait on a bulk-copy barrier gave up (the kernel drained its copies and
- * returned; results of that launch are incomplete).  Synchronises the device;
- * `reset` != 0 clears the word afterwards.  -1 if it could not be read.
+ * Status of the bounded waits on the current device: 0 = fine, else the code
+ * of a kernel that gave up waiting for its data (1 tile FFT kernels, 2
+ * tensor-core form, 3 TMA transpose) after draining its own copies; that
+ * launch's output is incomplete.  The word lives in pinned host memory, so
+ * every public entry point (dtfft_execute, dtfft_execute_noalloc,
+ * dtfft_transpose[_start], dtfft_reshape[_start], dtfft_gb_batch_execute,
+ * gb_kernel_execute, gb_fft_execute) reads it without synchronising and, if
+ * it is set, clears it and returns DTFFT_ERROR_GPU_WAIT_TIMEOUT before
+ * launching anything: a timeout is reported by the first call after the
+ * failed kernel has run.  This function synchronises the device first, so it
+ * reports a timeout of any kernel enqueued before it; `reset` != 0 clears the
+ * word afterwards.  -1 if the word could not be set up or the device failed.
  */
 int32_t dtfft_gb_device_status(int32_t reset);
+
+/**
+ * Iteration limit of the waits of the tile FFT kernels and the TMA transpose
+ * for their bulk copies, for kernels launched from now on (default 4194304,
+ * well over a second).  0 makes every such wait give up at once: the kernels
+ * then record status 1 or 3, wait (with the default bound) for the copies
+ * they issued and return, which is how the failure path is tested.  Returns
+ * DTFFT_ERROR_INVALID_USAGE for a negative value.
+ */
+int32_t dtfft_gb_set_wait_limit(int32_t iterations);
 
 /* ------------------------------------------------------------------------ */
 /* Kernel timing (for benchmarks)                                            */

@@ -156,39 +156,6 @@ def test_tile_schedules(dt, orc, cuda, dims, grid, np_dtype, inplace):
 
 
 @pytest.mark.parametrize("dims,grid,np_dtype", [
-    ([96, 40, 36], [1, 2, 2], np.complex64),         # M = 96: 4 threads per row, 8 rows per warp
-    ([160, 48, 20], [1, 2, 1], np.complex64),
-    ([384, 36, 10], [1, 3, 1], np.complex64),
-    ([48, 320, 288], [1, 1, 1], np.complex64),       # Z-slab plan on the fused generic route
-    ([100, 96, 160], [1, 1, 1], np.float32),         # R2C Z-slab plan on the fused generic route
-    ([120, 7, 3], [1, 1, 1], np.complex64),          # rows with a ragged last tile
-])
-def test_runtime_tile_kernels(dt, orc, cuda, monkeypatch, dims, grid, np_dtype):
-    """The opt-in runtime-schedule tile kernels (DTFFT_GB_RTILE=1): several rows
-    per warp, run-time radices, K w-slices per fused tile."""
-    monkeypatch.setenv("DTFFT_GB_RTILE", "1")
-    nd = len(dims)
-    if np_dtype == np.float32:
-        plan = dt.PlanR2C(dims, comm=comm_for(dt, grid), precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT)
-        cdt, kind = np.complex64, "r2c"
-    else:
-        plan = dt.PlanC2C(dims, comm=comm_for(dt, grid), precision=_prec(dt, np_dtype), executor=dt.Executor.CUFFT)
-        cdt, kind = np_dtype, "c2c"
-    g = random_global(tuple(dims[::-1]), np_dtype, seed=13)
-    x = orc.global_to_packed(g, nd, grid, 1)
-    a = to_dev(x, plan.alloc_size, cuda)
-    b = empty(plan.alloc_size, cdt, cuda)
-    plan.execute(a, b, dt.Execute.FORWARD)
-    expect = orc.global_to_packed(orc.forward_values(g, kind), nd, grid, _final_layout(plan, nd))
-    assert orc.rel_l2(from_dev(b, expect.size, cdt), expect) <= TOL[np_dtype]
-    c = empty(plan.alloc_size, np_dtype, cuda)
-    plan.execute(b, c, dt.Execute.BACKWARD)
-    back = from_dev(c, x.size, np_dtype) / np.prod(dims)
-    assert orc.rel_l2(back, x) <= TOL[np_dtype]
-    plan.destroy()
-
-
-@pytest.mark.parametrize("dims,grid,np_dtype", [
     ([512, 64, 32], [1, 2, 2], np.complex64),
     ([256, 48, 256], [1, 1, 2], np.complex128),
 ])
