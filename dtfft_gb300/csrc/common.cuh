@@ -116,6 +116,9 @@ int tma_tile_a(int elem);
 dtfft_error_t tma_launch(const BoxList& bl, const void* in, void* out, cudaStream_t s, int* status,
                          std::vector<std::pair<const void*, void*>>& cache);
 void tma_cache_free(std::vector<std::pair<const void*, void*>>& cache);
+// The driver's cuTensorMapEncodeTiled (PFN_cuTensorMapEncodeTiled_v12000), or
+// nullptr when it cannot be reached.
+void* tma_encode_tiled_fn();
 
 // Status word of the bounded waits on the current device (fft_host.cu): a
 // portable mapped host word per device, created by status_setup() when a

@@ -108,6 +108,10 @@ private:
     bool tile_ = false;
     int tile_nst_ = 0, tile_threads_ = 0, pair_ok_ = 0, ncw_ = 0, nsw_ = 0;
     const void* tw_bwd_ = nullptr;
+    // tensor-store write-out of the tile pass (fft_tile_xpose_tma_kernel);
+    // null when the pass's segments do not fit it or `use_xtma_` is off
+    struct XTma* xtma_ = nullptr;
+    bool use_xtma_ = false;
     Schedule sched_;
     const void* tw_ = nullptr;
     const void* groups_ = nullptr;

@@ -692,6 +692,69 @@ dtfft_error_t FftPlan::execute(const void* in, void* out, int sign, cudaStream_t
 // ---------------------------------------------------------------------------
 // FusedFT: batched C2C along the source's aligned axis + the box-list transpose
 // ---------------------------------------------------------------------------
+// Tensor-store write-out of a fused tile pass (fft_tile_xpose_tma_kernel):
+// the pass's source groups and destination segments, its launch shape, and
+// the tensor maps of the last few output buffers (a map holds the buffer's
+// address, so it is encoded on the host the first time a buffer is seen; a
+// pure host computation, also legal while a stream is being captured).
+struct XTma {
+    std::vector<FGroup> groups;
+    std::vector<FSeg> segs;
+    std::vector<int> seg_group;    // group of each segment
+    int nst = 0;
+    size_t smem = 0;
+    std::mutex mu;
+    std::vector<std::pair<const void*, TmaXMaps*>> maps;   // per output pointer, most recent last
+    ~XTma() { for (auto& e : maps) delete e.second; }
+};
+
+// Every store box of the pass fits the tensor-store kernel: segments start on
+// an 8-point boundary (the 128-byte swizzle of the staged lines repeats every
+// 8 lines), no box reads past the tile's M lines, destination base and strides
+// are 16-byte multiples, and the maps fit the kernel parameter.
+static bool xtma_fits(int m, int es, const std::vector<FSeg>& segs) {
+    if (segs.empty() || (int)segs.size() > kTmaXMaxSegs) return false;
+    for (const FSeg& sg : segs) {
+        const int len = sg.i1 - sg.i0;
+        if (len < 1 || sg.i0 % 8) return false;
+        const int box = std::min(len, 256);
+        for (int i = sg.i0; i < sg.i1; i += 256)
+            if (i + box > m) return false;
+        if ((sg.dst_off * es) % 16 || (sg.di * es) % 16 || (sg.dw * es) % 16) return false;
+        if (sg.di * es >= (1LL << 40) || sg.dw * es >= (1LL << 40) || sg.di < 1 || sg.dw < 0) return false;
+    }
+    return true;
+}
+
+// Tensor maps of every destination segment of the pass for output `out`:
+// (u in 8-byte words, i, w) of the segment's block, boxes of one 128-byte
+// line (u) by up to 256 points, 128-byte swizzle.
+static dtfft_error_t xtma_encode(const XTma& x, int es, void* out, TmaXMaps* mp) {
+    typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    EncodeFn enc = (EncodeFn)tma_encode_tiled_fn();
+    if (!enc) return DTFFT_ERROR_GPU_CALL_FAILED;
+    memset(mp, 0, sizeof(TmaXMaps));
+    const int w8 = es / 8;
+    for (size_t k = 0; k < x.segs.size(); ++k) {
+        const FSeg& sg = x.segs[k];
+        const FGroup& g = x.groups[x.seg_group[k]];
+        const int len = sg.i1 - sg.i0;
+        cuuint64_t gdim[3] = {(cuuint64_t)g.nu * w8, (cuuint64_t)len, (cuuint64_t)std::max(g.nw, 1)};
+        cuuint64_t gstr[2] = {(cuuint64_t)(sg.di * es), (cuuint64_t)(std::max<i64>(sg.dw, 1) * es)};
+        if (g.nw <= 1) gstr[1] = gstr[0] * (cuuint64_t)len;   // a single w plane: any stride does
+        cuuint32_t box[3] = {16, (cuuint32_t)std::min(len, 256), 1};
+        cuuint32_t estr[3] = {1, 1, 1};
+        void* base = (char*)out + sg.dst_off * es;
+        const CUresult r = enc(&mp->map[k], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, base, gdim, gstr, box, estr,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                               CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return DTFFT_ERROR_GPU_CALL_FAILED;
+    }
+    return DTFFT_SUCCESS;
+}
+
 dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only, FusedFT** out) {
     *out = nullptr;
     if (bl.copy || bl.host.empty()) return DTFFT_ERROR_INVALID_USAGE;
@@ -791,6 +854,33 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
                                  : TilePtr<float>::get(m, sg, true, p->ncw_, p->nsw_);
             err = set_smem_attrs(fn, ts.smem);
         }
+        // the tensor-store write-out when the pass's tiles are whole 128-byte
+        // lines and every segment fits it (the default then)
+        const void* fk = dbl ? TilePtr<double>::get_tma(m, -1) : TilePtr<float>::get_tma(m, -1);
+        const void* bk = dbl ? TilePtr<double>::get_tma(m, 1) : TilePtr<float>::get_tma(m, 1);
+        if (err == DTFFT_SUCCESS && fk && bk && ts.S * (int)es == 128 && tma_encode_tiled_fn() &&
+            xtma_fits(m, (int)es, segs)) {
+            XTma* x = new XTma();
+            x->groups = groups;
+            x->segs = segs;
+            for (size_t gi = 0; gi < groups.size(); ++gi)
+                for (int k = 0; k < groups[gi].nseg; ++k) x->seg_group.push_back((int)gi);
+            const size_t line_bytes = (size_t)m * 128;
+            x->nst = (int)std::min<size_t>(kTileMaxNst, (max_optin_smem() - 2 * kTileHdrXTma) / line_bytes);
+            x->smem = 2 * kTileHdrXTma + (size_t)x->nst * line_bytes;
+            // the driver validates the maps' shapes and strides when they are
+            // encoded: try once on an aligned stand-in address (host only)
+            TmaXMaps probe;
+            const bool encodable = xtma_encode(*x, (int)es, (void*)(uintptr_t)4096, &probe) == DTFFT_SUCCESS;
+            if (encodable && x->nst >= 2 && set_smem_attrs(fk, x->smem) == DTFFT_SUCCESS &&
+                set_smem_attrs(bk, x->smem) == DTFFT_SUCCESS) {
+                p->xtma_ = x;
+                p->use_xtma_ = true;
+            } else {
+                delete x;
+            }
+            cudaGetLastError();
+        }
     } else {
         const int pitch = m + m / 16;
         p->pitch_ = pitch;
@@ -829,7 +919,10 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
     return DTFFT_SUCCESS;
 }
 
-FusedFT::~FusedFT() { for (void* t : owned_) cudaFree(t); }
+FusedFT::~FusedFT() {
+    for (void* t : owned_) cudaFree(t);
+    delete xtma_;
+}
 
 template <typename R>
 static dtfft_error_t launch_fused_t(const FusedFT& F, int m, int E, int T, int S, int pitch, const Schedule& sch,
@@ -867,6 +960,43 @@ static dtfft_error_t launch_fused_pipe(int m, int E, int T, int S, int pitch, co
     void* tok = prof_begin(s);
     GB_TRY((launch_pipe<R, true>(P, E, S * T, smem, per_sm, s)));
     if (tok) prof_end(tok, std::string("fftpipe_xpose_m") + std::to_string(m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
+    count_launch();
+    GB_CUDA_TRY(cudaGetLastError());
+    return DTFFT_SUCCESS;
+}
+
+template <typename R>
+static dtfft_error_t launch_fused_tile_tma(int m, XTma& x, const void* tw, const void* groups, const void* segs,
+                                          int ngroups, i64 tiles, const void* in, void* out, int sign,
+                                          cudaStream_t s) {
+    typedef typename CT<R>::T C;
+    TXArgs<R> X;
+    TArgs<R>& P = X.a;
+    P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)tw;
+    P.nsig = 0; P.groups = (const FGroup*)groups; P.segs = (const FSeg*)segs; P.ngroups = ngroups;
+    P.ntiles = tiles; P.S = 128 / (int)sizeof(C); P.nst = x.nst; P.pair_ok = 0; P.wait_limit = g_wait_limit;
+    P.status = status_ptr();
+    {
+        std::lock_guard<std::mutex> lk(x.mu);
+        TmaXMaps* mp = nullptr;
+        for (auto& e : x.maps)
+            if (e.first == out) mp = e.second;
+        if (!mp) {
+            mp = new TmaXMaps();
+            const dtfft_error_t r = xtma_encode(x, (int)sizeof(C), out, mp);
+            if (r != DTFFT_SUCCESS) { delete mp; return r; }
+            if (x.maps.size() >= 4) { delete x.maps.front().second; x.maps.erase(x.maps.begin()); }
+            x.maps.emplace_back(out, mp);
+        }
+        memcpy(&X.m, mp, sizeof(TmaXMaps));
+    }
+    void (*kfn)(TXArgs<R>) = (void (*)(TXArgs<R>))TilePtr<R>::get_tma(m, sign);
+    if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    const i64 grid = std::min<i64>(tiles, (i64)sm_count());
+    const int threads = 32 * (128 / (int)sizeof(C) / 2 + 1);
+    void* tok = prof_begin(s);
+    kfn<<<(unsigned)grid, threads, x.smem, s>>>(X);
+    if (tok) prof_end(tok, std::string("ffttile_xtma_m") + std::to_string(m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);
     count_launch();
     GB_CUDA_TRY(cudaGetLastError());
     return DTFFT_SUCCESS;
@@ -917,6 +1047,12 @@ dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int i
     key << dev << "|" << m_ << "|" << dbl_ << "|" << S_ << "|" << ngroups_ << "|" << ctas_ << "|" << smem_;
     std::lock_guard<std::mutex> lk(g_ft_tune_mu);
     auto apply = [&](int c, int w) {
+        if (c < 0) {   // the tensor-store write-out
+            if (!xtma_) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+            use_xtma_ = true;
+            return DTFFT_SUCCESS;
+        }
+        use_xtma_ = false;
         ncw_ = c; nsw_ = w;
         const void* f = dbl_ ? TilePtr<double>::get(m_, -1, true, c, w) : TilePtr<float>::get(m_, -1, true, c, w);
         int threads = 0;
@@ -939,15 +1075,16 @@ dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int i
         return DTFFT_SUCCESS;   // keep the default split when scratch is not available
     }
     cudaMemsetAsync(a, 0, bytes, s);
-    static const int cands[][2] = {{0, 0}, {3, 5}, {4, 4}, {2, 6}, {4, 8}, {6, 6}, {8, 4}};
+    static const int cands[][2] = {{-1, -1}, {0, 0}, {3, 5}, {4, 4}, {2, 6}, {4, 8}, {6, 6}, {8, 4}};
     int best_c = 0, best_w = 0;
     float best_ms = 1e30f;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     for (const auto& c : cands) {
-        const bool have = c[0] == 0 || (dbl_ ? TilePtr<double>::get(m_, -1, true, c[0], c[1])
-                                             : TilePtr<float>::get(m_, -1, true, c[0], c[1])) != nullptr;
+        const bool have = c[0] == 0 || (c[0] < 0 && xtma_) ||
+                          (c[0] > 0 && (dbl_ ? TilePtr<double>::get(m_, -1, true, c[0], c[1])
+                                             : TilePtr<float>::get(m_, -1, true, c[0], c[1])) != nullptr);
         if (!have || apply(c[0], c[1]) != DTFFT_SUCCESS) continue;
         bool ok = true;
         for (int i = 0; i < warmup && ok; ++i) ok = execute(a, b, -1, s) == DTFFT_SUCCESS;
@@ -959,7 +1096,10 @@ dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int i
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         ms /= (float)std::max(iters, 1);
-        if (log) printf("dtFFT-gb300: fused pass m=%d warps %d+%d: %.4f ms\n", m_, c[0], c[1], ms);
+        if (log) {
+            if (c[0] < 0) printf("dtFFT-gb300: fused pass m=%d tensor-store write-out: %.4f ms\n", m_, ms);
+            else printf("dtFFT-gb300: fused pass m=%d warps %d+%d: %.4f ms\n", m_, c[0], c[1], ms);
+        }
         if (ms < best_ms) { best_ms = ms; best_c = c[0]; best_w = c[1]; }
     }
     cudaEventDestroy(e0);
@@ -977,6 +1117,11 @@ dtfft_error_t FusedFT::execute(const void* in, void* out, int sign, cudaStream_t
     if (tile_) {
         if (((uintptr_t)in % 16) != 0 || ((uintptr_t)out % 16) != 0) return DTFFT_ERROR_INVALID_USAGE;
         const void* tw = sign > 0 ? tw_bwd_ : tw_;
+        if (use_xtma_ && xtma_) {
+            if (dbl_)
+                return launch_fused_tile_tma<double>(m_, *xtma_, tw, groups_, segs_, ngroups_, ctas_, in, out, sign, s);
+            return launch_fused_tile_tma<float>(m_, *xtma_, tw, groups_, segs_, ngroups_, ctas_, in, out, sign, s);
+        }
         if (dbl_)
             return launch_fused_tile<double>(m_, S_, tile_nst_, tile_threads_, ncw_, nsw_, smem_, pair_ok_, tw, groups_,
                                              segs_, ngroups_, ctas_, in, out, sign, s);

@@ -40,6 +40,8 @@
 // copies still in flight before it returns.
 #pragma once
 
+#include <cuda.h>
+
 #include "fft_kernels.cuh"
 
 namespace gb {
@@ -491,6 +493,182 @@ __global__ void __launch_bounds__(32 * (NCW + NSW), 1) fft_tile_xpose_kernel(TAr
     }
 }
 
+// ---------------------------------------------------------------------------
+// Rows fused with the transpose, written out by TMA tensor stores
+// ---------------------------------------------------------------------------
+// The same pass as fft_tile_xpose_kernel with the write-out moved off the SMs:
+//  - each compute warp transforms a pair of adjacent rows (u, u + 1) of the
+//    tile, keeping both spectra in registers;
+//  - after a barrier of the compute warps (every row of the tile has been read
+//    and its exchanges are done) the warps write the tile back into its own
+//    buffer transposed, [point i][row u] with u fastest: one 128-byte line per
+//    point (S rows of 8 or 16 bytes), 16-byte stores of the row pair,
+//    128-byte swizzled (16-byte chunk c of line i at chunk c ^ (i mod 8));
+//  - one producer warp issues the bulk loads, and per destination segment
+//    the cp.async.bulk.tensor stores of the transposed lines (boxes of
+//    S rows x up to 256 points, the tensor map un-swizzles them), then reuses
+//    the buffer for the next load once the store has read it.
+// No thread of the SM executes a global store; each point leaves as part of a
+// 128-byte line of the destination rank's block.
+constexpr int kTmaXMaxSegs = 48;
+constexpr int kTileHdrXTma = 1024;   // header; the launch adds another 1 KB of alignment slack
+
+struct TmaXMaps {
+    CUtensorMap map[kTmaXMaxSegs];   // per destination segment: (u words, i, w) of its block
+};
+
+template <typename R>
+struct TXArgs {
+    TArgs<R> a;
+    TmaXMaps m;
+};
+
+__device__ __forceinline__ bool bar_red_or(int id, int nthreads, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.or.pred p, %2, %3, q;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id), "r"(nthreads)
+        : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ void bar_sync_n(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* smem, int c0, int c1, int c2) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(map),
+                 "r"(smem_u32(smem)), "r"(c0), "r"(c1), "r"(c2)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+template <typename R, int SG, int NCW, int E, int... Rs>
+__global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(const __grid_constant__ TXArgs<R> X) {
+    typedef typename CT<R>::T C;
+    constexpr int M = (Rs * ... * 1);
+    constexpr int ES = (int)sizeof(C);
+    constexpr int S = 128 / ES;                 // rows per tile: one 128-byte line per point
+    static_assert(M == E * 32, "one warp per row");
+    static_assert(M % 16 == 0, "swizzles need 16-point blocks");
+    static_assert(2 * NCW == S, "one row pair per compute warp");
+    const TArgs<R>& A = X.a;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // full[b]: the load into buffer b landed; done[b]: the compute warps wrote
+    // buffer b back transposed
+    // the swizzle pattern of the staged lines is anchored at 1024-byte
+    // boundaries: align the start of the header (the launch adds 1 KB of slack)
+    unsigned char* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    uint64_t* full = reinterpret_cast<uint64_t*>(base);
+    uint64_t* done = full + kTileMaxNst;
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(base + 16 * kTileMaxNst);
+    unsigned char* ring = base + kTileHdrXTma;              // 1024-byte aligned buffers of M lines
+    const int NST = A.nst;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < NST; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&done[b], NCW);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp < NCW) {
+        // ---- compute warps: rows 2*warp and 2*warp + 1 of every tile ----
+        Tw2<R, E, Rs...> t2;
+        t2.load(lane, A.tw);
+        Tw3<R, E, Rs...> t3;
+        t3.load(lane, A.tw);
+        const int ua = 2 * warp;
+        int b = 0;
+        uint32_t par = 0;
+        for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+            const bool ok = mbar_wait_or_abort(&full[b], par, abort_flag, A.wait_limit);
+            if (bar_red_or(1, 32 * NCW, !ok)) {
+                if (threadIdx.x == 0) { report_status(A.status, 1); *abort_flag = 1; }
+                return;
+            }
+            i64 row0, rs;
+            int nrows, gi, u0, w;
+            tile_geom<R, true, M>(A, tile, row0, rs, nrows, gi, u0, w);
+            C* tb = reinterpret_cast<C*>(ring + (size_t)b * M * 128);
+            C va[E], vb[E];
+            if (ua < nrows) tile_row_fft<R, SG, E, Rs...>(va, tb + ua * M, lane, A.tw, t2, t3);
+            if (ua + 1 < nrows) tile_row_fft<R, SG, E, Rs...>(vb, tb + (ua + 1) * M, lane, A.tw, t2, t3);
+            // every row of the tile has been read: the buffer takes the transposed lines
+            bar_sync_n(2, 32 * NCW);
+            unsigned char* lines = reinterpret_cast<unsigned char*>(tb);
+#pragma unroll
+            for (int q = 0; q < E; ++q) {
+                const int i = lane + 32 * q;
+                unsigned char* line = lines + (size_t)i * 128;
+                if constexpr (ES == 8) {
+                    // rows ua, ua + 1 share the 16-byte chunk `warp`
+                    float4 v;
+                    v.x = va[q].x; v.y = va[q].y; v.z = vb[q].x; v.w = vb[q].y;
+                    *reinterpret_cast<float4*>(line + ((warp ^ (i & 7)) << 4)) = v;
+                } else {
+                    // one 16-byte chunk per row
+                    *reinterpret_cast<C*>(line + ((ua ^ (i & 7)) << 4)) = va[q];
+                    *reinterpret_cast<C*>(line + (((ua + 1) ^ (i & 7)) << 4)) = vb[q];
+                }
+            }
+            // the tensor stores read the buffer through the async proxy
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&done[b]);
+            if (++b == NST) { b = 0; par ^= 1; }
+        }
+        return;
+    }
+
+    // ---- producer warp: bulk loads in, tensor stores out ----
+    if (lane != 0) return;
+    uint32_t issued_par = 0;   // bit b: parity of the last load into buffer b
+    for (int j = 0; j < NST; ++j) {
+        const i64 tj = blockIdx.x + (i64)j * gridDim.x;
+        if (tj < A.ntiles) tile_issue<R, true, M>(A, tj, reinterpret_cast<C*>(ring + (size_t)j * M * 128), &full[j]);
+    }
+    int b = 0;
+    uint32_t par = 0;
+    bool failed = false;
+    for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+        if (!mbar_wait_or_abort(&done[b], par, abort_flag)) { failed = true; break; }
+        i64 row0, rs;
+        int nrows, gi, u0, w;
+        tile_geom<R, true, M>(A, tile, row0, rs, nrows, gi, u0, w);
+        const unsigned char* tb = ring + (size_t)b * M * 128;
+        const FGroup& g = A.groups[gi];
+        for (int kk = 0; kk < g.nseg; ++kk) {
+            const FSeg sg = A.segs[g.seg_first + kk];
+            const CUtensorMap* map = &X.m.map[g.seg_first + kk];
+            for (int i = sg.i0; i < sg.i1; i += 256)
+                tma_store_3d(map, tb + (size_t)i * 128, u0 * (ES / 8), i - sg.i0, w);
+        }
+        bulk_commit();
+        // the store has read the buffer: refill it
+        bulk_wait_read_all();
+        const i64 tn = tile + (i64)NST * gridDim.x;
+        if (tn < A.ntiles) {
+            tile_issue<R, true, M>(A, tn, reinterpret_cast<C*>(ring + (size_t)b * M * 128), &full[b]);
+            issued_par = (issued_par & ~(1u << b)) | ((par ^ 1u) << b);
+        }
+        if (++b == NST) { b = 0; par ^= 1; }
+    }
+    if (failed) {
+        report_status(A.status, 1);
+        *abort_flag = 1;
+        // wait (bounded) for the last load issued into every buffer
+        for (int j = 0; j < NST && blockIdx.x + (i64)j * gridDim.x < A.ntiles; ++j)
+            mbar_wait_bounded(&full[j], (issued_par >> j) & 1u);
+    }
+    bulk_wait_all();
+}
+
 // Tile-kernel entry points of one precision (fft_tile_f32.cu / fft_tile_f64.cu):
 // nullptr when no variant is compiled for M.
 template <typename R>
@@ -500,6 +678,8 @@ struct TilePtr {
     static void* get(int M, int sign, bool xpose, int ncw = 0, int nsw = 0);
     static int points_per_thread(int M);   // E of the compiled variants, 0 if none
     static int default_threads(int M, bool xpose);
+    // fused kernel with tensor-store write-out (fft_tile_xpose_tma_kernel), nullptr if none for M
+    static void* get_tma(int M, int sign);
 };
 
 }  // namespace gb

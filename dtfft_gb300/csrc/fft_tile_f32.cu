@@ -40,6 +40,24 @@ void* TilePtr<float>::get(int M, int sign, bool xpose, int ncw, int nsw) {
 #undef GB_PLAIN
 #undef GB_XPOSE
 
+// Fused passes with the tensor-store write-out: 8 compute warps (one row
+// pair each of a 16-row tile) + 1 producer warp.
+template <>
+void* TilePtr<float>::get_tma(int M, int sign) {
+    switch (M) {
+    case 256:
+        return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<float, -1, 8, 8, 8, 8, 4>
+                        : (void*)fft_tile_xpose_tma_kernel<float, 1, 8, 8, 8, 8, 4>;
+    case 512:
+        return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<float, -1, 8, 16, 16, 16, 2>
+                        : (void*)fft_tile_xpose_tma_kernel<float, 1, 8, 16, 16, 16, 2>;
+    case 768:
+        return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<float, -1, 8, 24, 8, 8, 4, 3>
+                        : (void*)fft_tile_xpose_tma_kernel<float, 1, 8, 24, 8, 8, 4, 3>;
+    }
+    return nullptr;
+}
+
 template <>
 int TilePtr<float>::points_per_thread(int M) {
     switch (M) {

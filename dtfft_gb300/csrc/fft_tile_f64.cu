@@ -22,6 +22,21 @@ void* TilePtr<double>::get(int M, int sign, bool xpose, int ncw, int nsw) {
     return nullptr;
 }
 
+// Fused passes with the tensor-store write-out: 4 compute warps (one row
+// pair each of an 8-row tile) + 1 producer warp.
+template <>
+void* TilePtr<double>::get_tma(int M, int sign) {
+    switch (M) {
+    case 256:
+        return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<double, -1, 4, 8, 8, 8, 4>
+                        : (void*)fft_tile_xpose_tma_kernel<double, 1, 4, 8, 8, 8, 4>;
+    case 512:
+        return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<double, -1, 4, 16, 16, 16, 2>
+                        : (void*)fft_tile_xpose_tma_kernel<double, 1, 4, 16, 16, 16, 2>;
+    }
+    return nullptr;
+}
+
 template <>
 int TilePtr<double>::points_per_thread(int M) {
     switch (M) {

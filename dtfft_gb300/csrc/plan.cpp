@@ -352,6 +352,16 @@ int32_t dtfft_vgrid_world_create(int32_t nprocs, MPI_Comm* comm) {
     return DTFFT_SUCCESS;
 }
 
+int32_t dtfft_vgrid_comm_size(MPI_Comm comm, int32_t* size) {
+    if (!size) return DTFFT_ERROR_INVALID_USAGE;
+    if (comm == MPI_COMM_WORLD || comm == MPI_COMM_SELF) { *size = 1; return DTFFT_SUCCESS; }
+    VComm v;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!lookup_comm(comm, v)) return DTFFT_ERROR_INVALID_COMM_TYPE;
+    *size = v.nprocs;
+    return DTFFT_SUCCESS;
+}
+
 int32_t dtfft_vgrid_free(MPI_Comm* comm) {
     if (!comm) return DTFFT_ERROR_INVALID_USAGE;
     std::lock_guard<std::mutex> lk(g_mu);

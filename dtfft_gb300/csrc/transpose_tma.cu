@@ -148,6 +148,8 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return g_encode_fn;
 }
 
+void* tma_encode_tiled_fn() { return (void*)encode_fn(); }
+
 // Boxes of this list fit the TMA kernel: 8- or 16-byte elements, at most
 // kTmaMaxBoxes boxes, every box start and source stride 16-byte aligned.
 bool tma_eligible(const BoxList& bl) {

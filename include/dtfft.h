@@ -29,8 +29,16 @@
 
 #include "dtfft_mpi_shim.h"
 
+/* What the reference's generated dtfft_config.h defines for a CUDA build with
+ * both GPU executors: both executor names select this library's kernels. */
 #ifndef DTFFT_WITH_CUDA
 #define DTFFT_WITH_CUDA
+#endif
+#ifndef DTFFT_WITH_CUFFT
+#define DTFFT_WITH_CUFFT
+#endif
+#ifndef DTFFT_WITH_VKFFT
+#define DTFFT_WITH_VKFFT
 #endif
 
 #ifdef __cplusplus

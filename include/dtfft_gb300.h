@@ -250,6 +250,14 @@ void dtfft_gb_profile_stop(void);
 int32_t dtfft_gb_profile_count(void);
 int32_t dtfft_gb_profile_get(int32_t index, char* name, int32_t name_len, int64_t* launches, double* total_ms);
 
+/**
+ * Measured FP64 FMA throughput of the current device in TFLOP/s (independent
+ * FMA chains on every SM, best of 4 timed launches): the roofline of the
+ * complex128 / float64 transforms, whose kernels are bound by the FP64 pipe.
+ * Synchronises the device.
+ */
+int32_t dtfft_gb_measure_fp64_fma(double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

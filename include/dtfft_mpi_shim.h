@@ -81,6 +81,13 @@ int32_t dtfft_vgrid_world_create(int32_t nprocs, MPI_Comm* comm);
 int32_t dtfft_vgrid_pencils_create(int32_t nprocs, int32_t ndims, const int32_t* starts, const int32_t* counts,
                                    MPI_Comm* comm);
 
+/**
+ * Number of virtual ranks a handle stands for: 1 for MPI_COMM_WORLD and
+ * MPI_COMM_SELF, prod(dims) for a cartesian grid, `nprocs` for the others.
+ * DTFFT_ERROR_INVALID_COMM_TYPE for an unknown handle.
+ */
+int32_t dtfft_vgrid_comm_size(MPI_Comm comm, int32_t* size);
+
 /** Releases a handle made by dtfft_vgrid_cart_create or dtfft_vgrid_world_create. */
 int32_t dtfft_vgrid_free(MPI_Comm* comm);
 

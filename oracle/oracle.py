@@ -385,3 +385,105 @@ def choose_grid(ndims, gdims, nprocs=1, z_slab=True, y_slab=False, cart=None):
             if a >= b and (best is None or a - b < best[0] - best[1]):
                 best = (a, b)
     return [1, best[0], best[1]], False, False
+
+
+# ----------------------------------------------------------------------------
+# Full-size checks: packed positions and sampled spectrum lines (FP64)
+# ----------------------------------------------------------------------------
+
+def packed_index(ndims, gdims, grid, layout, coords) -> np.ndarray:
+    """Positions in the packed multi-rank buffer of layout `layout` of the
+    global points `coords` (array (n, ndims) of (x, y[, z]) indices): rank r's
+    block starts at rank_offset and stores its pencil aligned-axis-first
+    (src/dtfft_transpose_plan.F90:1084-1131)."""
+    coords = np.asarray(coords, dtype=np.int64).reshape(-1, ndims)
+    grid = norm_grid(ndims, grid)
+    # global axis held by pencil dim d of this layout
+    if ndims == 2:
+        axes = [0, 1] if layout == 1 else [1, 0]
+    else:
+        axes = {1: [0, 1, 2], 2: [1, 2, 0], 3: [2, 0, 1]}[layout]
+    out = np.full(len(coords), -1, dtype=np.int64)
+    for r in range(nranks(ndims, grid)):
+        s, c = pencil(ndims, gdims, grid, layout, r)
+        loc = np.stack([coords[:, axes[d]] - s[d] for d in range(ndims)], axis=1)
+        inside = np.all((loc >= 0) & (loc < np.asarray(c)[None, :]), axis=1)
+        if not inside.any():
+            continue
+        lin = np.zeros(int(inside.sum()), dtype=np.int64)
+        stride = 1
+        for d in range(ndims):
+            lin += loc[inside, d] * stride
+            stride *= c[d]
+        out[inside] = rank_offset(ndims, gdims, grid, layout, r) + lin
+    if (out < 0).any():
+        raise ValueError("a point lies outside every rank's block")
+    return out
+
+
+def _basis(n, k, kind, axis_kind):
+    """Column k of the forward transform of length n along one axis:
+    exp(-2 pi i j k / n) for C2C and R2C axes, FFTW's r2r kernels otherwise."""
+    if axis_kind == "dft":
+        return np.exp(-2j * np.pi * np.arange(n) * k / n)
+    m = r2r_direct(np.eye(n), kind)
+    return m[:, k]
+
+
+def _line_transform(v, n_out, axis_kind, kind):
+    if axis_kind == "dft":
+        return np.fft.fft(v)[:n_out]
+    return r2r(np.real(v), kind, axis=-1)
+
+
+def sampled_lines(g: np.ndarray, kind: str, axis: int, points, kinds=None, chunk=16):
+    """FP64 values of the forward 3D transform of `g` (numpy C order [z][y][x],
+    FFTW conventions as forward_values) along `axis` (0 = X, 1 = Y, 2 = Z) at
+    the fixed output indices `points` of the two other axes, in X, Y, Z order
+    ((ky, kz) for X lines, (kx, kz) for Y lines, (kx, ky) for Z lines).
+
+    The transform is separable, so each line is the contraction of g with the
+    basis vectors of the two fixed indices followed by the 1D transform along
+    `axis`; g is read once per call in chunks of `chunk` z-planes, which keeps
+    inputs of several GiB within host memory.  R2C: X is the halved axis
+    (n/2 + 1 outputs), the others are C2C.  Returns (len(points), n_axis_out)."""
+    nz, ny, nx = g.shape
+    n = [nx, ny, nz]
+    other = [a for a in range(3) if a != axis]
+    pts = [tuple(int(v) for v in p) for p in points]
+    K = len(pts)
+
+    def axis_kind(a):
+        return "r2r" if kind == "r2r" else "dft"
+
+    def kind_of(a):
+        return kinds[a] if kind == "r2r" else None
+
+    dt_acc = np.float64 if kind == "r2r" else np.complex128
+    bases = {a: np.stack([_basis(n[a], p[i], kind_of(a), axis_kind(a)) for p in pts], axis=1).astype(dt_acc)
+             for i, a in enumerate(other)}
+    acc = np.zeros((K, n[axis]), dtype=dt_acc)
+    for z0 in range(0, nz, chunk):
+        G = np.asarray(g[z0:z0 + chunk]).astype(dt_acc)          # (cz, ny, nx)
+        cz = G.shape[0]
+        if axis == 2:          # contract x, then y
+            T = (G.reshape(-1, nx) @ bases[0]).reshape(cz, ny, K)
+            acc[:, z0:z0 + cz] = np.einsum("zyk,yk->kz", T, bases[1])
+        elif axis == 1:        # contract x, then z
+            T = (G.reshape(-1, nx) @ bases[0]).reshape(cz, ny, K)
+            acc += np.einsum("zyk,zk->ky", T, bases[2][z0:z0 + cz])
+        else:                  # contract y, then z
+            T = np.matmul(G.transpose(0, 2, 1), bases[1])      # (cz, nx, K)
+            acc += np.einsum("zxk,zk->kx", T, bases[2][z0:z0 + cz])
+    n_out = n[axis] // 2 + 1 if (kind == "r2c" and axis == 0) else n[axis]
+    return np.stack([_line_transform(acc[i], n_out, axis_kind(axis), kind_of(axis)) for i in range(K)])
+
+
+def line_coords(axis: int, point, n_axis: int) -> np.ndarray:
+    """Global (x, y, z) indices of one sampled line (see sampled_lines)."""
+    other = [a for a in range(3) if a != axis]
+    c = np.zeros((n_axis, 3), dtype=np.int64)
+    c[:, axis] = np.arange(n_axis)
+    c[:, other[0]] = point[0]
+    c[:, other[1]] = point[1]
+    return c

@@ -217,3 +217,44 @@ def test_cpu_port_computes_the_transform(orc, dims, grid):
     assert orc.rel_l2(y[:expect.size], expect) <= 1e-5
     back = plan.backward(y)[:x.size] / np.prod(dims)
     assert orc.rel_l2(back, x) <= 1e-5
+
+
+@pytest.mark.parametrize("kind", ["c2c", "r2c", "r2r"])
+def test_sampled_lines_equal_full_transform(orc, kind):
+    """The separable line oracle used at full sizes equals the full FP64
+    transform on every sampled line, for lines along each axis."""
+    rng = np.random.default_rng(7)
+    shape = (10, 12, 14)
+    g = rng.standard_normal(shape) + (1j * rng.standard_normal(shape) if kind == "c2c" else 0)
+    kinds = [orc.DCT_2, orc.DST_3, orc.DCT_4] if kind == "r2r" else None
+    F = orc.forward_values(g, kind, kinds)          # [kz][ky][kx]
+    nx_out = F.shape[2]
+    for axis, pts in ((0, [(1, 2), (5, 9)]), (1, [(3, 4), (0, 7)]), (2, [(2, 11), (4, 0)])):
+        lines = orc.sampled_lines(g, kind, axis, pts, kinds, chunk=3)
+        for i, p in enumerate(pts):
+            if axis == 0:
+                ref = F[p[1], p[0], :]
+            elif axis == 1:
+                ref = F[p[1], :, p[0]]
+            else:
+                ref = F[:, p[1], p[0]]
+            assert lines[i].shape == ref.shape
+            np.testing.assert_allclose(lines[i], ref, rtol=0, atol=1e-12 * np.abs(F).max())
+    assert nx_out == (8 if kind == "r2c" else 14)
+
+
+def test_packed_index_matches_global_to_packed(orc):
+    rng = np.random.default_rng(8)
+    dims, grid = [10, 12, 14], [1, 2, 3]
+    g = rng.standard_normal(tuple(dims[::-1]))
+    co = np.stack(np.meshgrid(np.arange(10), np.arange(12), np.arange(14), indexing="ij"), -1).reshape(-1, 3)
+    for lay in (1, 2, 3):
+        p = orc.global_to_packed(g, 3, grid, lay)
+        idx = orc.packed_index(3, dims, grid, lay, co)
+        assert np.array_equal(p[idx], g[co[:, 2], co[:, 1], co[:, 0]])
+    g2 = rng.standard_normal((9, 11))
+    co2 = np.stack(np.meshgrid(np.arange(11), np.arange(9), indexing="ij"), -1).reshape(-1, 2)
+    for lay in (1, 2):
+        p = orc.global_to_packed(g2, 2, [1, 3], lay)
+        idx = orc.packed_index(2, [11, 9], [1, 3], lay, co2)
+        assert np.array_equal(p[idx], g2[co2[:, 1], co2[:, 0]])

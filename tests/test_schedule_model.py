@@ -168,3 +168,42 @@ def test_tma_transpose_tile_coverage(ES):
             w, r, TA, TB = tma_tile_writes(ES, ra, rb)
             assert sorted(w) == sorted((a, b) for a in range(ra) for b in range(rb))
             assert all(0 <= x and x + 16 <= 4 * TB * 128 for x in r)
+
+
+def _tma_unswizzle_128b(offset):
+    """Byte offset inside a 1024-byte aligned staging buffer that the 128-byte
+    tensor-map swizzle reads for logical byte `offset` of the box: the 16-byte
+    chunk index (bits 4..6) is XORed with the 128-byte line index mod 8 (bits 7..9)."""
+    return offset ^ (((offset >> 7) & 7) << 4)
+
+
+@pytest.mark.parametrize("es,M", [(8, 256), (8, 512), (8, 768), (16, 256), (16, 512)])
+def test_tensor_store_staging_matches_the_map_swizzle(es, M):
+    """fft_tile_xpose_tma_kernel: compute warp w writes rows (2w, 2w+1) of
+    point i into line i at chunk (pair ^ (i & 7)) (complex64: one 16-byte chunk
+    per row pair; complex128: one chunk per row).  The tensor store of a box of
+    lines [i0, i0 + L) with i0 % 8 == 0, read through the 128-byte swizzle, must
+    deliver element (u, i) of the destination block from where row u's value of
+    point i was written, for every (u, i), each staging byte used once."""
+    S = 128 // es
+    ncw = S // 2
+    written = {}
+    for w in range(ncw):
+        ua = 2 * w
+        for i in range(M):
+            line = i * 128
+            if es == 8:
+                off = line + ((w ^ (i & 7)) << 4)
+                written[off] = (ua, i)
+                written[off + 8] = (ua + 1, i)
+            else:
+                written[line + ((ua ^ (i & 7)) << 4)] = (ua, i)
+                written[line + (((ua + 1) ^ (i & 7)) << 4)] = (ua + 1, i)
+    assert len(written) == S * M                         # every (row, point) once
+    for i0 in range(0, M, 128):
+        L = min(256, M - i0)
+        for i in range(i0, i0 + L):
+            for u in range(S):
+                logical = (i - i0) * 128 + u * es         # box element (u, i): u fastest, 128-byte lines
+                phys = _tma_unswizzle_128b(i0 * 128 + logical)
+                assert written[phys] == (u, i)

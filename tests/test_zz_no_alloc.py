@@ -111,7 +111,10 @@ def test_noalloc_matches_execute_bit_for_bit(dt, cuda, case):
         plan.execute(a, ref, direction)                 # existing entry point, plan-owned aux
         torch.cuda.synchronize()
         ref_h = ref.cpu().numpy()
-        assert np.isfinite(ref_h).all()
+        # the layout the direction ends in is finite; buffer space past it stays NaN in both runs
+        _, in_counts, _, out_counts, _ = plan.local_sizes
+        n_valid = int(np.prod(out_counts if direction == dt.Execute.FORWARD else in_counts))
+        assert np.isfinite(ref_h[:n_valid]).all()
         for call in range(2):
             _poison_scratch(dt, L, cuda)
             a = src.clone()
