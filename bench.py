@@ -199,6 +199,28 @@ def batch_shapes(count=64, seed=5):
     return [("c2c" if i % 2 == 0 else "r2c", [int(rng.choice(edges)) for _ in range(3)]) for i in range(count)]
 
 
+def _tune_records(dt):
+    """Summary of the FFT step autotuner's choices (EXHAUSTIVE plans): steps
+    tuned, chosen kernel kinds, and the chosen and runner-up candidates with
+    their times for the steps where the choice mattered most."""
+    L = dt.lib()
+    L.dtfft_gb_tune_records.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    n = ctypes.c_size_t()
+    if L.dtfft_gb_tune_records(None, 0, ctypes.byref(n)) != 0:
+        return None
+    buf = ctypes.create_string_buffer(n.value)
+    if L.dtfft_gb_tune_records(buf, n.value, ctypes.byref(n)) != 0:
+        return None
+    recs = json.loads(buf.value.decode())
+    kinds = {}
+    for r in recs:
+        k = r["chosen"].split(":")[0]
+        kinds[k] = kinds.get(k, 0) + 1
+    gain = sorted(recs, key=lambda r: -(r["runner_up_ms"] - r["chosen_ms"]) if r["runner_up"] else 0)
+    return {"steps_tuned": len(recs), "candidates_timed": sum(r["candidates"] for r in recs),
+            "chosen_kinds": kinds, "largest_margins": gain[:12]}
+
+
 def batched_section(args, dt, dev, stream, peak):
     """64 mixed transforms, fwd+bwd each: 64 sequential plain plans (default
     effort, one dtfft_execute per plan and direction) against the same
@@ -232,6 +254,7 @@ def batched_section(args, dt, dev, stream, peak):
         pass_bytes += 2 * passes * 2 * cbytes
     dt.set_config(dt.Config())
     torch.cuda.synchronize()
+    tune = _tune_records(dt)
     ins = [b[0] for b in bufs]
     outs = [b[1] for b in bufs]
     auxs = [b[2] for b in bufs]
@@ -299,6 +322,7 @@ def batched_section(args, dt, dev, stream, peak):
             "speedup": seq_ms / batch_ms,
             "sequential_kernel_classes": kernel_classes,
             "unfused_pass_bytes_per_cycle": pass_bytes,
+            "fft_autotune": tune,
             "effective_tbs": {"sequential_plain": pass_bytes / (seq_ms * 1e-3) / 1e12,
                               "batched_graph": pass_bytes / (batch_ms * 1e-3) / 1e12}}
 

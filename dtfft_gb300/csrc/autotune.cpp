@@ -83,7 +83,7 @@ dtfft_error_t autotune_boxes(BoxList& bl, i64 max_elems, cudaStream_t s, int war
     }
     cudaMemsetAsync(a, 0, bytes, s);
     static const TransposeConfig cands[] = {
-        {32, 32, 8}, {32, 32, 4}, {64, 32, 8}, {32, 64, 8}, {64, 64, 8}, {64, 64, 16}};
+        {32, 32, 8}, {32, 32, 4}, {64, 32, 8}, {32, 64, 8}, {64, 64, 8}, {64, 64, 16}, {128, 32, 8}};
     TransposeConfig best = bl.cfg;
     float best_ms = 1e30f;
     cudaEvent_t e0, e1;
@@ -91,13 +91,17 @@ dtfft_error_t autotune_boxes(BoxList& bl, i64 max_elems, cudaStream_t s, int war
     cudaEventCreate(&e1);
     for (const TransposeConfig& c : cands) {
         if (bl.elem == 16 && c.tile_a * c.tile_b > 32 * 64) continue;  // static smem limit
+        // 128 x 32 exists only as the TMA kernel of 4-byte elements
+        if (c.tile_a == 128 && !(bl.elem == 4 && tma_eligible(bl))) continue;
         bl.cfg = c;
         if (boxes_upload(bl) != DTFFT_SUCCESS) continue;
-        for (int i = 0; i < warmup; ++i) boxes_launch(bl, a, b, s);
+        bool ok = true;
+        for (int i = 0; i < warmup && ok; ++i) ok = boxes_launch(bl, a, b, s) == DTFFT_SUCCESS;
         cudaEventRecord(e0, s);
-        for (int i = 0; i < iters; ++i) boxes_launch(bl, a, b, s);
+        for (int i = 0; i < iters && ok; ++i) ok = boxes_launch(bl, a, b, s) == DTFFT_SUCCESS;
         cudaEventRecord(e1, s);
         cudaEventSynchronize(e1);
+        if (!ok) { cudaGetLastError(); continue; }
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         ms /= (float)iters;

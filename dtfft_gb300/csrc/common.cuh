@@ -113,6 +113,7 @@ dtfft_error_t boxes_launch(const BoxList& bl, const void* in, void* out, cudaStr
 // extent along a, the launch, and the release of a list's tensor maps.
 bool tma_eligible(const BoxList& bl);
 int tma_tile_a(int elem);
+void tma_default_tile(BoxList& bl);
 dtfft_error_t tma_launch(const BoxList& bl, const void* in, void* out, cudaStream_t s, int* status,
                          std::vector<std::pair<const void*, void*>>& cache);
 void tma_cache_free(std::vector<std::pair<const void*, void*>>& cache);

@@ -67,6 +67,9 @@ public:
     dtfft_error_t execute(const void* in, void* out, int sign, cudaStream_t s);
     const FftDesc& desc() const { return d_; }
     int launches_per_execute() const { return launches_; }
+    // Measured choice of each step's kernel, tile shape and radix schedule
+    // (EXHAUSTIVE plans); cached per GPU and step geometry.
+    dtfft_error_t autotune(cudaStream_t s, int warmup, int iters, bool log);
 
 private:
     FftDesc d_;

@@ -690,6 +690,350 @@ dtfft_error_t FftPlan::execute(const void* in, void* out, int sign, cudaStream_t
 }
 
 // ---------------------------------------------------------------------------
+// Measured choice of every FFT step's kernel and schedule (EXHAUSTIVE plans)
+// ---------------------------------------------------------------------------
+// Replaces the reference's NVRTC block optimizer for the FFT side
+// (src/dtfft_nvrtc_block_optimizer.F90:502-751 scores candidates analytically,
+// src/dtfft_kernel_device.F90:259-411 times them under EXHAUSTIVE): for each
+// step the candidates are
+//   tile   the warp-per-row tile kernel (C2C rows of a compiled length) with
+//          S rows per tile and a ring of nst tiles,
+//   reg    the register kernel for every compiled points-per-thread count E
+//          and several radix orders, with 256 / T or 128 / T signals per CTA,
+//   pipe   the same register schedules on the bulk-copy pipelined kernel,
+//   smem   the shared-memory kernel,
+// each timed with CUDA events on scratch buffers of the step's footprint; the
+// fastest is kept.  Choices are cached per (GPU, library version, step
+// geometry) in the process and, with DTFFT_GB_TUNE_CACHE, in that file.
+struct StepCand {
+    enum Kind { TILE, PIPE, REG, SMEM } kind = SMEM;
+    int E = 0, per = 1, S = 0, nst = 0;
+    std::vector<int> radix;
+    std::string name() const {
+        std::ostringstream o;
+        switch (kind) {
+        case TILE: o << "tile:S" << S << ":nst" << nst; break;
+        case SMEM: o << "smem"; break;
+        default: {
+            o << (kind == PIPE ? "pipe:E" : "reg:E") << E << ":";
+            for (size_t i = 0; i < radix.size(); ++i) o << (i ? "x" : "") << radix[i];
+            o << ":per" << per;
+        }
+        }
+        return o.str();
+    }
+    static bool parse(const std::string& t, StepCand& c) {
+        c = StepCand();
+        if (t == "smem") { c.kind = SMEM; return true; }
+        if (t.compare(0, 5, "tile:") == 0) {
+            c.kind = TILE;
+            return sscanf(t.c_str(), "tile:S%d:nst%d", &c.S, &c.nst) == 2;
+        }
+        const bool pipe = t.compare(0, 5, "pipe:") == 0;
+        if (!pipe && t.compare(0, 4, "reg:") != 0) return false;
+        c.kind = pipe ? PIPE : REG;
+        const size_t a = t.find(":E"), b = t.find(':', a + 2), d = t.find(":per");
+        if (a == std::string::npos || b == std::string::npos || d == std::string::npos) return false;
+        c.E = atoi(t.c_str() + a + 2);
+        c.per = atoi(t.c_str() + d + 4);
+        std::string rs = t.substr(b + 1, d - b - 1);
+        for (size_t i = 0; i <= rs.size();) {
+            size_t j = rs.find('x', i);
+            if (j == std::string::npos) j = rs.size();
+            c.radix.push_back(atoi(rs.substr(i, j - i).c_str()));
+            i = j + 1;
+        }
+        return c.E > 0 && c.per > 0;
+    }
+};
+
+// Greedy radix schedule of m for points-per-thread E with a radix preference.
+static bool greedy_schedule(int m, int E, const std::vector<int>& pref, std::vector<int>& out) {
+    out.clear();
+    int r = m;
+    while (r > 1) {
+        int pick = 0;
+        for (int q : pref)
+            if (E % q == 0 && r % q == 0) { pick = q; break; }
+        if (!pick) return false;
+        out.push_back(pick);
+        r /= pick;
+    }
+    return !out.empty() || m == 1;
+}
+
+// Set a step up for one candidate; false when the candidate cannot run.
+static bool apply_cand(FftStep& S, const StepCand& c, std::vector<void*>& owned) {
+    const size_t es = S.dbl ? 16 : 8;
+    const int m = S.m;
+    const bool c2c_rows = !S.cols && S.mode == M_C2C && S.idist == m && S.odist == m;
+    S.tile = false;
+    S.pipe = false;
+    switch (c.kind) {
+    case StepCand::TILE: {
+        if (!c2c_rows) return false;
+        const void* fn = S.dbl ? TilePtr<double>::get(m, S.sign, false) : TilePtr<float>::get(m, S.sign, false);
+        if (!fn) return false;
+        const size_t smem = kTileHdrPlain + (size_t)c.nst * c.S * m * es;
+        if (c.nst < 2 || c.nst > kTileMaxNst || smem > max_optin_smem()) return false;
+        if (set_smem_attrs(fn, smem) != DTFFT_SUCCESS) { cudaGetLastError(); return false; }
+        if (!S.tw_dir && upload_dir_table(m, S.sign, S.dbl, owned, &S.tw_dir) != DTFFT_SUCCESS) return false;
+        const int dthreads = S.dbl ? TilePtr<double>::default_threads(m, false) : TilePtr<float>::default_threads(m, false);
+        S.tile = true;
+        S.tile_S = c.S; S.tile_nst = c.nst; S.tile_nw = 0;
+        S.tile_threads = std::min(dthreads, 32 * c.S);
+        S.tile_smem = smem;
+        return true;
+    }
+    case StepCand::REG:
+    case StepCand::PIPE: {
+        const bool c2c = S.mode == M_C2C;
+        const void* fn = S.dbl ? KPtr<double>::reg(c.E, S.cols, c2c) : KPtr<float>::reg(c.E, S.cols, c2c);
+        if (!fn || m % c.E) return false;
+        int prod = 1;
+        for (int r : c.radix) { if (c.E % r) return false; prod *= r; }
+        if (prod != m) return false;
+        const int T = m / c.E;
+        if (c.per < 1 || c.per * T > 1024) return false;
+        S.E = c.E;
+        S.sched.m = m;
+        S.sched.radix = c.radix;
+        S.per = c.per;
+        S.threads = c.per * T;
+        S.pitch = m + m / 16;
+        S.smem = S.cols ? (size_t)m * c.per * es : (size_t)c.per * S.pitch * es;
+        if (S.smem > max_optin_smem() || set_smem_attrs(fn, S.smem) != DTFFT_SUCCESS) { cudaGetLastError(); return false; }
+        if (c.kind == StepCand::PIPE) {
+            if (!c2c_rows || (m * es) % 16) return false;
+            S.pipe_smem = 128 + 2 * (size_t)c.per * m * es + S.smem;
+            if (S.pipe_smem > max_optin_smem()) return false;
+            S.pipe_ctas_per_sm = pipe_occupancy(S.dbl, m, c.E, false, S.threads, S.pipe_smem);
+            if (S.pipe_ctas_per_sm <= 0) return false;
+            S.pipe = true;
+        }
+        return true;
+    }
+    case StepCand::SMEM: {
+        Schedule sc;
+        if (!make_schedule(m, sc)) return false;
+        const size_t per_sig = 2 * (size_t)m * es;
+        if (per_sig > 220 * 1024) return false;
+        S.E = 0;
+        S.sched = sc;
+        int per;
+        if (S.cols) {
+            per = S.dbl ? 8 : 16;
+            while (per > 1 && per * per_sig > 200 * 1024) per >>= 1;
+            per = (int)std::min<i64>(per, S.ncols);
+            S.pitch = per;
+        } else {
+            per = (int)std::max<size_t>(1, kSmemBudget / per_sig);
+            i64 want = std::max<i64>(1, S.nsig / (152 * 4));
+            per = (int)std::max<i64>(1, std::min<i64>(per, want));
+            per = std::min(per, 64);
+            S.pitch = m;
+        }
+        S.per = std::max(1, per);
+        S.smem = (size_t)S.per * per_sig;
+        const void* fn = S.dbl ? KPtr<double>::generic(S.cols) : KPtr<float>::generic(S.cols);
+        if (set_smem_attrs(fn, S.smem) != DTFFT_SUCCESS) { cudaGetLastError(); return false; }
+        return true;
+    }
+    }
+    return false;
+}
+
+static std::vector<StepCand> step_candidates(const FftStep& S) {
+    std::vector<StepCand> out;
+    const int m = S.m;
+    const size_t es = S.dbl ? 16 : 8;
+    const bool c2c_rows = !S.cols && S.mode == M_C2C && S.idist == m && S.odist == m;
+    if (c2c_rows && (S.dbl ? TilePtr<double>::get(m, S.sign, false) : TilePtr<float>::get(m, S.sign, false))) {
+        for (int sr : {16, 8, 4, 2}) {
+            if (sr > (S.dbl ? 8 : 16)) continue;
+            const int maxn = (int)std::min<size_t>(kTileMaxNst, (max_optin_smem() - kTileHdrPlain) / ((size_t)sr * m * es));
+            for (int nst : {2, 3, 4, maxn}) {
+                if (nst < 2 || nst > maxn) continue;
+                StepCand c;
+                c.kind = StepCand::TILE; c.S = sr; c.nst = nst;
+                bool dup = false;
+                for (const StepCand& o : out) dup = dup || (o.kind == c.kind && o.S == c.S && o.nst == c.nst);
+                if (!dup) out.push_back(c);
+            }
+        }
+    }
+    static const std::vector<int> Es_f32 = {8, 16, 24, 20, 28, 7, 9, 10, 12, 14, 15, 18, 21, 25, 30, 35, 42};
+    static const std::vector<int> Es_f64 = {8, 16, 24, 20, 28, 7, 9, 10, 12, 14, 15, 18, 21, 25};
+    static const std::vector<std::vector<int>> prefs = {
+        {16, 8, 7, 5, 4, 3, 2}, {8, 16, 7, 5, 4, 3, 2}, {7, 5, 3, 16, 8, 4, 2}, {4, 8, 16, 7, 5, 3, 2}};
+    for (int E : S.dbl ? Es_f64 : Es_f32) {
+        if (m % E) continue;
+        const int T = m / E;
+        if (T > 256 || (S.cols && T > 64)) continue;
+        std::vector<std::vector<int>> scheds;
+        for (const auto& pf : prefs) {
+            std::vector<int> r;
+            if (!greedy_schedule(m, E, pf, r)) continue;
+            bool dup = false;
+            for (const auto& o : scheds) dup = dup || o == r;
+            if (!dup) scheds.push_back(r);
+        }
+        for (const auto& r : scheds) {
+            for (int per : {256 / T, 128 / T}) {
+                if (per < 1) continue;
+                StepCand c;
+                c.kind = StepCand::REG; c.E = E; c.radix = r; c.per = per;
+                out.push_back(c);
+                if (c2c_rows && (m * es) % 16 == 0) { c.kind = StepCand::PIPE; out.push_back(c); }
+                if (256 / T == 128 / T) break;
+            }
+        }
+    }
+    Schedule sc;
+    if (make_schedule(m, sc)) out.push_back(StepCand());   // smem
+    return out;
+}
+
+static std::string library_gpu_name() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return "unknown";
+    std::string s = prop.name;
+    for (char& c : s) if (c == ' ' || c == '|' || c == '\t') c = '_';
+    return s;
+}
+
+static std::string step_key(const FftStep& S) {
+    std::ostringstream o;
+    o << library_gpu_name() << "|v" << DTFFT_VERSION_CODE << "|" << S.dbl << "|" << S.mode << "|" << (S.cols ? 1 : 0)
+      << "|" << S.n << "|" << S.m << "|" << S.nsig << "|" << S.idist << "|" << S.odist << "|" << S.plane << "|" << S.ld
+      << "|" << S.ncols;
+    return o.str();
+}
+
+struct TuneRecord {
+    std::string step, best, second;
+    float best_ms = 0, second_ms = 0;
+    int candidates = 0;
+};
+
+static std::mutex g_step_tune_mu;
+static std::map<std::string, std::string> g_step_tune;   // key -> candidate name
+static bool g_step_tune_loaded = false;
+static std::vector<TuneRecord> g_tune_records;
+
+static void step_tune_load() {
+    if (g_step_tune_loaded) return;
+    g_step_tune_loaded = true;
+    const char* path = getenv("DTFFT_GB_TUNE_CACHE");
+    if (!path) return;
+    FILE* f = fopen(path, "r");
+    if (!f) return;
+    char tag[16], key[512], val[256];
+    while (fscanf(f, "%15s %511s %255s", tag, key, val) == 3) {
+        if (strcmp(tag, "fft1") == 0) g_step_tune[key] = val;
+        else { int ch; while ((ch = fgetc(f)) != '\n' && ch != EOF) {} }
+    }
+    fclose(f);
+}
+
+static void step_tune_store(const std::string& key, const std::string& val) {
+    const char* path = getenv("DTFFT_GB_TUNE_CACHE");
+    if (!path) return;
+    if (FILE* f = fopen(path, "a")) {
+        fprintf(f, "fft1 %s %s\n", key.c_str(), val.c_str());
+        fclose(f);
+    }
+}
+
+// Bytes a step touches from the start of its input and output buffers.
+static size_t step_bytes(const FftStep& S) {
+    const size_t es = S.dbl ? 16 : 8;
+    i64 elems;
+    if (S.cols) elems = (S.nsig / std::max(S.ncols, 1) + 1) * S.plane + S.ld;
+    else elems = S.nsig * std::max<i64>(std::max(S.idist, S.odist), S.m) + 2 * (i64)S.m + 2;
+    return (size_t)elems * es;
+}
+
+dtfft_error_t FftPlan::autotune(cudaStream_t s, int warmup, int iters, bool log) {
+    std::lock_guard<std::mutex> lk(g_step_tune_mu);
+    step_tune_load();
+    for (std::vector<FftStep*>* dir : {&fwd_, &bwd_}) {
+        for (FftStep* S : *dir) {
+            if (S->tc || S->blue) continue;
+            const std::string key = step_key(*S);
+            StepCand chosen;
+            auto it = g_step_tune.find(key);
+            if (it != g_step_tune.end() && StepCand::parse(it->second, chosen)) {
+                FftStep t = *S;
+                t.tc = nullptr; t.blue = nullptr;
+                if (apply_cand(t, chosen, tables_)) { *S = t; t.tc = nullptr; t.blue = nullptr; }
+                continue;
+            }
+            const size_t bytes = step_bytes(*S);
+            if (bytes > (size_t)4 << 30) continue;   // keep the default for very large steps
+            void *a = nullptr, *b = nullptr;
+            if (cudaMalloc(&a, bytes) != cudaSuccess || cudaMalloc(&b, bytes) != cudaSuccess) {
+                cudaGetLastError();
+                if (a) cudaFree(a);
+                continue;
+            }
+            cudaMemsetAsync(a, 0, bytes, s);
+            cudaMemsetAsync(b, 0, bytes, s);
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            const std::vector<StepCand> cands = step_candidates(*S);
+            const FftStep orig = *S;
+            TuneRecord rec;
+            rec.step = std::string(S->cols ? "cols" : "rows") + "_m" + std::to_string(S->m) + "_mode" +
+                       std::to_string(S->mode) + (S->dbl ? "_f64" : "_f32") + "_n" + std::to_string(S->nsig);
+            float best = 1e30f, second = 1e30f;
+            StepCand best_c, second_c;
+            bool any = false;
+            for (const StepCand& c : cands) {
+                FftStep t = orig;
+                t.tc = nullptr; t.blue = nullptr;
+                if (!apply_cand(t, c, tables_)) { t.tc = nullptr; t.blue = nullptr; continue; }
+                bool ok = true;
+                for (int i = 0; i < warmup && ok; ++i) ok = launch_step(t, a, b, s) == DTFFT_SUCCESS;
+                cudaEventRecord(e0, s);
+                for (int i = 0; i < iters && ok; ++i) ok = launch_step(t, a, b, s) == DTFFT_SUCCESS;
+                cudaEventRecord(e1, s);
+                const bool synced = cudaEventSynchronize(e1) == cudaSuccess;
+                t.tc = nullptr; t.blue = nullptr;
+                if (!ok || !synced) { cudaGetLastError(); continue; }
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms /= (float)std::max(iters, 1);
+                ++rec.candidates;
+                if (log) printf("dtFFT-gb300: fft step %s %s: %.4f ms\n", rec.step.c_str(), c.name().c_str(), ms);
+                if (ms < best) { second = best; second_c = best_c; best = ms; best_c = c; any = true; }
+                else if (ms < second) { second = ms; second_c = c; }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            cudaStreamSynchronize(s);
+            cudaFree(a);
+            cudaFree(b);
+            cudaGetLastError();
+            if (!any) continue;
+            FftStep t = orig;
+            t.tc = nullptr; t.blue = nullptr;
+            if (apply_cand(t, best_c, tables_)) { *S = t; }
+            t.tc = nullptr; t.blue = nullptr;
+            rec.best = best_c.name(); rec.best_ms = best;
+            if (second < 1e29f) { rec.second = second_c.name(); rec.second_ms = second; }
+            g_tune_records.push_back(rec);
+            g_step_tune[key] = rec.best;
+            step_tune_store(key, rec.best);
+        }
+    }
+    return DTFFT_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
 // FusedFT: batched C2C along the source's aligned axis + the box-list transpose
 // ---------------------------------------------------------------------------
 // Tensor-store write-out of a fused tile pass (fft_tile_xpose_tma_kernel):
@@ -1151,6 +1495,25 @@ extern "C" int32_t dtfft_gb_device_status(int32_t reset) {
     const int v = *w;
     if (reset) *w = 0;
     return v;
+}
+
+extern "C" int32_t dtfft_gb_tune_records(char* buf, size_t cap, size_t* len) {
+    std::lock_guard<std::mutex> lk(gb::g_step_tune_mu);
+    std::ostringstream o;
+    o << "[";
+    for (size_t i = 0; i < gb::g_tune_records.size(); ++i) {
+        const gb::TuneRecord& r = gb::g_tune_records[i];
+        o << (i ? "," : "") << "{\"step\":\"" << r.step << "\",\"chosen\":\"" << r.best << "\",\"chosen_ms\":" << r.best_ms
+          << ",\"runner_up\":\"" << r.second << "\",\"runner_up_ms\":" << r.second_ms
+          << ",\"candidates\":" << r.candidates << "}";
+    }
+    o << "]";
+    const std::string t = o.str();
+    if (len) *len = t.size() + 1;
+    if (!buf) return DTFFT_SUCCESS;
+    if (cap < t.size() + 1) return DTFFT_ERROR_INVALID_USAGE;
+    memcpy(buf, t.c_str(), t.size() + 1);
+    return DTFFT_SUCCESS;
 }
 
 extern "C" int32_t dtfft_gb_set_wait_limit(int32_t iterations) {

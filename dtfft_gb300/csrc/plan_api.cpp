@@ -140,6 +140,7 @@ static dtfft_error_t build_transposes(Plan& p) {
         BoxList& bl = p.tr[t + 3];
         bl = make_boxes(p.pen[send_layout(t) - 1], p.pen[recv_layout(t) - 1], p.elem);
         bl.cfg = default_tile(p.elem);
+        tma_default_tile(bl);
         GB_TRY(boxes_upload(bl));
     }
     return DTFFT_SUCCESS;
@@ -346,6 +347,10 @@ static dtfft_error_t create_plan(int kind, int8_t ndims, const int32_t* dims, co
             if (!f || e != DTFFT_SUCCESS) continue;
             const i64 elems = p->kind == K_R2C ? p->alloc_size() / 2 : p->alloc_size();   // transformed elements
             e = f->autotune(elems, p->stream, cfg.n_measure_warmup_iters, cfg.n_measure_iters, p->log);
+        }
+        for (FftPlan* f : p->fft) {
+            if (!f || e != DTFFT_SUCCESS) continue;
+            e = f->autotune(p->stream, cfg.n_measure_warmup_iters, cfg.n_measure_iters, p->log);
         }
     }
     if (e != DTFFT_SUCCESS) { delete p; return e; }

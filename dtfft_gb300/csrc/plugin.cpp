@@ -155,6 +155,7 @@ dtfft_error_t gb_kernel_create(int32_t ndims, const int32_t* dims, int32_t base_
         }
     }
     if (e == DTFFT_SUCCESS && !k->all.host.empty()) {
+        if (!k->all.copy) tma_default_tile(k->all);
         e = boxes_upload(k->all);
         for (auto& b : k->per) if (e == DTFFT_SUCCESS) e = boxes_upload(b);
         if (e == DTFFT_SUCCESS && effort == DTFFT_EXHAUSTIVE) {

@@ -1,8 +1,8 @@
-// Box-list transpose with TMA tensor loads (8- and 16-byte elements).
+// Box-list transpose with TMA tensor loads (4-, 8- and 16-byte elements).
 //
 // Each box of a virtual-grid transpose, src[src_off + a + b*sb + c*sc] ->
 // dst[dst_off + b + a*da + c*dc], is described by a 3D tensor map over
-// (a, b, c).  A CTA owns one 64 x 32 (8-byte) or 32 x 32 (16-byte) (a, b)
+// (a, b, c).  A CTA owns one 128 x 32 (4-byte), 64 x 32 (8-byte) or 32 x 32 (16-byte) (a, b)
 // tile of one c-plane: one thread issues four cp.async.bulk.tensor loads of
 // 128-byte-wide boxes, which land in shared memory with the 128-byte swizzle
 // (16-byte chunk index XOR row index mod 8) and complete on an mbarrier.  The
@@ -82,11 +82,13 @@ __global__ void __launch_bounds__(256) box_transpose_tma_kernel(const __grid_con
         const CUtensorMap* map = &P.maps[lo];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            // the map counts a in 8-byte words: x = element index * (ES / 8), always even
+            // the map counts a in 8-byte words (4-byte elements: in elements):
+            // x = element index * (ES / 8), always even (a multiple of 32 for 4 bytes)
             asm volatile(
                 "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
                 " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(tma_smem_u32(tile + k * TB * 128)),
-                "l"(map), "r"((a0 + k * IN) * (ES / 8)), "r"(b0), "r"(c), "r"(tma_smem_u32(&bar))
+                "l"(map), "r"(ES >= 8 ? (a0 + k * IN) * (ES / 8) : (a0 + k * IN)), "r"(b0), "r"(c),
+                "r"(tma_smem_u32(&bar))
                 : "memory");
         }
     }
@@ -108,7 +110,20 @@ __global__ void __launch_bounds__(256) box_transpose_tma_kernel(const __grid_con
     if (b >= rb) return;
     char* dst = out + (bx.dst_off + (i64)c * bx.dc + b0 + b) * ES;
     const i64 da = bx.da_or_db * ES;
-    if constexpr (ES == 8) {
+    if constexpr (ES == 4) {
+        // thread: row b, the 16-byte chunk holding a .. a + 3
+        for (int aq = warp; aq < TA / 4; aq += 8) {
+            const int a = 4 * aq;
+            if (a >= ra) break;
+            const int k = a / IN, ai = a % IN;
+            const int chunk = ((ai * ES) >> 4) ^ (b & 7);
+            const uint4 v = *reinterpret_cast<const uint4*>(tile + k * TB * 128 + b * 128 + chunk * 16);
+            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (a + j < ra) *reinterpret_cast<uint32_t*>(dst + (i64)(a0 + a + j) * da) = w4[j];
+        }
+    } else if constexpr (ES == 8) {
         // thread: row b, the 16-byte chunk holding a and a + 1
         for (int ap = warp; ap < TA / 2; ap += 8) {
             const int a = 2 * ap;
@@ -153,7 +168,8 @@ void* tma_encode_tiled_fn() { return (void*)encode_fn(); }
 // Boxes of this list fit the TMA kernel: 8- or 16-byte elements, at most
 // kTmaMaxBoxes boxes, every box start and source stride 16-byte aligned.
 bool tma_eligible(const BoxList& bl) {
-    if (bl.copy || (bl.elem != 8 && bl.elem != 16) || bl.host.empty() || (int)bl.host.size() > kTmaMaxBoxes)
+    if (bl.copy || (bl.elem != 4 && bl.elem != 8 && bl.elem != 16) || bl.host.empty() ||
+        (int)bl.host.size() > kTmaMaxBoxes)
         return false;
     if (getenv("DTFFT_GB_NO_TMA")) return false;
     for (const Box& x : bl.host)
@@ -164,6 +180,16 @@ bool tma_eligible(const BoxList& bl) {
 
 // tile extents of the TMA kernel (a x b)
 int tma_tile_a(int elem) { return 4 * (128 / elem); }
+
+// The default tile of a list: the TMA kernel's extents for 4-byte elements when
+// the list fits it (8- and 16-byte defaults already are the TMA extents).
+void tma_default_tile(BoxList& bl) {
+    if (bl.elem == 4 && tma_eligible(bl)) {
+        bl.cfg.tile_a = tma_tile_a(4);
+        bl.cfg.tile_b = 32;
+        bl.cfg.rows = 8;
+    }
+}
 
 static std::mutex g_tma_mu;
 
@@ -184,14 +210,14 @@ dtfft_error_t tma_launch(const BoxList& bl, const void* in, void* out, cudaStrea
             P = new TmaParams();
             memset(P, 0, sizeof(TmaParams));
             const int es = bl.elem;
-            const CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_UINT64;   // 8-byte words
+            // 8-byte words (16-byte elements are two words along a); 4-byte elements as themselves
+            const CUtensorMapDataType dt = es == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32 : CU_TENSOR_MAP_DATA_TYPE_UINT64;
             for (size_t i = 0; i < bl.host.size(); ++i) {
                 const Box& x = bl.host[i];
-                // 16-byte elements are two 8-byte words along a
-                const int w = es / 8;
-                cuuint64_t gdim[3] = {(cuuint64_t)x.na * w, (cuuint64_t)x.nb, (cuuint64_t)x.nc};
+                const cuuint64_t na = es == 4 ? (cuuint64_t)x.na : (cuuint64_t)x.na * (es / 8);
+                cuuint64_t gdim[3] = {na, (cuuint64_t)x.nb, (cuuint64_t)x.nc};
                 cuuint64_t gstr[2] = {(cuuint64_t)(x.sb * es), (cuuint64_t)(x.sc * es)};
-                cuuint32_t box[3] = {16, 32, 1};
+                cuuint32_t box[3] = {es == 4 ? 32u : 16u, 32, 1};
                 cuuint32_t estr[3] = {1, 1, 1};
                 void* base = (char*)in + x.src_off * es;
                 CUresult r = encode_fn()(&P->maps[i], dt, 3, base, gdim, gstr, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -209,7 +235,8 @@ dtfft_error_t tma_launch(const BoxList& bl, const void* in, void* out, cudaStrea
     L.wait_limit = g_wait_limit;
     L.boxes = bl.dev;   // re-read: an autotune re-upload may have moved the list
     if (bl.total_tiles == 0) return DTFFT_SUCCESS;
-    if (bl.elem == 8) box_transpose_tma_kernel<8><<<(unsigned)bl.total_tiles, 256, 0, s>>>(L, (char*)out);
+    if (bl.elem == 4) box_transpose_tma_kernel<4><<<(unsigned)bl.total_tiles, 256, 0, s>>>(L, (char*)out);
+    else if (bl.elem == 8) box_transpose_tma_kernel<8><<<(unsigned)bl.total_tiles, 256, 0, s>>>(L, (char*)out);
     else box_transpose_tma_kernel<16><<<(unsigned)bl.total_tiles, 256, 0, s>>>(L, (char*)out);
     return DTFFT_SUCCESS;
 }

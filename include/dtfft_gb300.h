@@ -251,6 +251,16 @@ int32_t dtfft_gb_profile_count(void);
 int32_t dtfft_gb_profile_get(int32_t index, char* name, int32_t name_len, int64_t* launches, double* total_ms);
 
 /**
+ * Choices of the FFT step autotuner so far in this process (plans created with
+ * DTFFT_EXHAUSTIVE or enable_kernel_autotune time every candidate kernel, tile
+ * shape and radix schedule of each FFT step): a JSON array of
+ * {"step", "chosen", "chosen_ms", "runner_up", "runner_up_ms", "candidates"}.
+ * `len` receives the bytes needed (with the terminating zero); buf = NULL only
+ * queries it.  DTFFT_ERROR_INVALID_USAGE when `cap` is too small.
+ */
+int32_t dtfft_gb_tune_records(char* buf, size_t cap, size_t* len);
+
+/**
  * Measured FP64 FMA throughput of the current device in TFLOP/s (independent
  * FMA chains on every SM, best of 4 timed launches): the roofline of the
  * complex128 / float64 transforms, whose kernels are bound by the FP64 pipe.

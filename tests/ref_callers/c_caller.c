@@ -21,7 +21,7 @@
 #include "helpers.h"
 
 static void c2c_double(void) {
-    int32_t dims[3] = {40, 48, 64};   /* slowest first: nz, ny, nx */
+    int32_t dims[3] = {40, 48, 64};   /* dims[0] is the fastest axis, as in dtFFT's C API */
     dtfft_plan_t plan;
     DTFFT_CALL(dtfft_create_plan_c2c(3, dims, MPI_COMM_WORLD, DTFFT_DOUBLE, DTFFT_ESTIMATE, DTFFT_EXECUTOR_VKFFT, &plan))
     int32_t in_counts[3], out_counts[3];
@@ -67,7 +67,8 @@ static void r2c_float(void) {
     DTFFT_CALL(dtfft_get_alloc_bytes(plan, &alloc_bytes))
     const size_t in_size = (size_t)in_counts[0] * in_counts[1] * in_counts[2];
     const size_t out_size = (size_t)out_counts[0] * out_counts[1] * out_counts[2];
-    if (out_counts[0] != 96 / 2 + 1 && out_counts[2] != 96 / 2 + 1 && out_counts[1] != 96 / 2 + 1)
+    /* dims[0] is the fastest axis: the Fourier-space layout holds 32 / 2 + 1 points of it */
+    if (out_counts[0] != 32 / 2 + 1 && out_counts[1] != 32 / 2 + 1 && out_counts[2] != 32 / 2 + 1)
         MPI_Abort(MPI_COMM_WORLD, 2);
     float *in, *out;
     cudaMallocManaged((void**)&in, alloc_bytes, cudaMemAttachGlobal);

@@ -23,7 +23,7 @@
 using namespace dtfft;
 
 static void r2r_float_3d() {
-    const std::vector<int32_t> dims = {20, 24, 32};   // slowest first
+    const std::vector<int32_t> dims = {20, 24, 32};   // dims[0] is the fastest axis
     const std::vector<R2RKind> kinds = {R2RKind::DCT_2, R2RKind::DST_2, R2RKind::DCT_3};
     PlanR2R plan(dims, kinds, MPI_COMM_WORLD, Precision::SINGLE, Effort::ESTIMATE, Executor::VKFFT);
     if (plan.get_precision() != Precision::SINGLE || plan.get_executor() != Executor::VKFFT) MPI_Abort(MPI_COMM_WORLD, 11);

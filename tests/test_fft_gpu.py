@@ -508,3 +508,48 @@ def test_plans_release_device_memory(dt, cuda):
         torch.cuda.empty_cache()
     free1, _ = torch.cuda.mem_get_info()
     assert free0 - free1 < 64 << 20, f"{(free0 - free1) >> 20} MiB not returned"
+
+
+@pytest.mark.parametrize("kind,dims,np_dtype", [
+    ("c2c", [70, 48, 105], np.complex64),
+    ("r2c", [60, 42, 35], np.float32),
+    ("c2c", [512, 24, 40], np.complex128),
+    ("r2r", [40, 36, 30], np.float64),
+])
+def test_exhaustive_fft_step_autotune(dt, orc, cuda, kind, dims, np_dtype):
+    """EXHAUSTIVE plans time every candidate kernel / tile shape / radix
+    schedule of each FFT step (dtfft_gb_tune_records lists the choices) and
+    still compute the oracle's spectrum."""
+    import ctypes
+    prec = dt.Precision.SINGLE if np_dtype in (np.complex64, np.float32) else dt.Precision.DOUBLE
+    L = dt.lib()
+    L.dtfft_gb_tune_records.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    n0 = ctypes.c_size_t()
+    assert L.dtfft_gb_tune_records(None, 0, ctypes.byref(n0)) == 0
+    kinds = None
+    if kind == "c2c":
+        plan = dt.PlanC2C(dims, precision=prec, executor=dt.Executor.CUFFT, effort=dt.Effort.EXHAUSTIVE)
+        cdt = np_dtype
+    elif kind == "r2c":
+        plan = dt.PlanR2C(dims, precision=prec, executor=dt.Executor.CUFFT, effort=dt.Effort.EXHAUSTIVE)
+        cdt = np.complex64
+    else:
+        kinds = [dt.R2RKind.DCT_2, dt.R2RKind.DST_4, dt.R2RKind.DCT_1]
+        plan = dt.PlanR2R(dims, kinds, precision=prec, executor=dt.Executor.VKFFT, effort=dt.Effort.EXHAUSTIVE)
+        cdt = np_dtype
+    n1 = ctypes.c_size_t()
+    assert L.dtfft_gb_tune_records(None, 0, ctypes.byref(n1)) == 0
+    buf = ctypes.create_string_buffer(n1.value)
+    assert L.dtfft_gb_tune_records(buf, n1.value, ctypes.byref(n1)) == 0
+    import json
+    recs = json.loads(buf.value.decode())
+    assert recs and all(r["chosen_ms"] > 0 for r in recs)
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=23, dist="normal")
+    x = orc.global_to_packed(g, 3, [1, 1, 1], 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, cdt, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    ok = [int(k) for k in kinds] if kinds else None
+    expect = orc.global_to_packed(orc.forward_values(g, kind, ok), 3, [1, 1, 1], _final_layout(plan, 3))
+    assert orc.rel_l2(from_dev(b, expect.size, cdt), expect) <= TOL[np_dtype]
+    plan.destroy()

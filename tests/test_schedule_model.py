@@ -138,7 +138,18 @@ def tma_tile_writes(ES, ra, rb):
         b = lane
         if b >= rb:
             continue
-        if ES == 8:
+        if ES == 4:
+            for aq in range(warp, TA // 4, 8):
+                a = 4 * aq
+                if a >= ra:
+                    break
+                k, ai = a // IN, a % IN
+                chunk = ((ai * ES) >> 4) ^ (b & 7)
+                reads.append(k * TB * 128 + b * 128 + chunk * 16)
+                for j in range(4):
+                    if a + j < ra:
+                        writes.append((a + j, b))
+        elif ES == 8:
             for ap in range(warp, TA // 2, 8):
                 a = 2 * ap
                 if a >= ra:
@@ -160,7 +171,7 @@ def tma_tile_writes(ES, ra, rb):
     return writes, reads, TA, TB
 
 
-@pytest.mark.parametrize("ES", [8, 16])
+@pytest.mark.parametrize("ES", [4, 8, 16])
 def test_tma_transpose_tile_coverage(ES):
     IN = 128 // ES
     for ra in sorted({1, 3, IN, 4 * IN - 1, 4 * IN}):
