@@ -759,7 +759,7 @@ def run_ours(args):
 
     tensor_core = None
     if not args.no_tc:
-        tensor_core = tensor_core_section(args, dt, dev, stream)
+        tensor_core = tensor_core_section(args, dt, dev, stream, sizes=tuple(args.tc_sizes))
 
     cfg1 = cfg3 = None
     if not args.no_configs:
@@ -831,6 +831,8 @@ def main():
     ap.add_argument("--no-transpose-only", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-transform batched section")
     ap.add_argument("--no-tc", action="store_true", help="skip the tensor-core 768^3 / 1024^3 section")
+    ap.add_argument("--tc-sizes", type=int, nargs="+", default=[768, 1024],
+                    help="cube edges of the tensor-core section (smaller ones for profiling)")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the 2D c128 256x256 and R2C/R2R f64 1024x1024x512 sections")
     ap.add_argument("--dims", type=int, nargs=3, default=None,

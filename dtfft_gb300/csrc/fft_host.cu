@@ -747,6 +747,10 @@ struct StepCand {
     }
 };
 
+// DCT/DST-II and -III through an n/2-point complex FFT: only the register
+// kernels implement these modes.
+static bool half_mode(int mode) { return mode == M_DCT2H || mode == M_DST2H || mode == M_DCT3H || mode == M_DST3H; }
+
 // Greedy radix schedule of m for points-per-thread E with a radix preference.
 static bool greedy_schedule(int m, int E, const std::vector<int>& pref, std::vector<int>& out) {
     out.clear();
@@ -815,7 +819,7 @@ static bool apply_cand(FftStep& S, const StepCand& c, std::vector<void*>& owned)
     }
     case StepCand::SMEM: {
         Schedule sc;
-        if (!make_schedule(m, sc)) return false;
+        if (half_mode(S.mode) || !make_schedule(m, sc)) return false;
         const size_t per_sig = 2 * (size_t)m * es;
         if (per_sig > 220 * 1024) return false;
         S.E = 0;
@@ -890,7 +894,7 @@ static std::vector<StepCand> step_candidates(const FftStep& S) {
         }
     }
     Schedule sc;
-    if (make_schedule(m, sc)) out.push_back(StepCand());   // smem
+    if (make_schedule(m, sc) && !half_mode(S.mode)) out.push_back(StepCand());   // smem
     return out;
 }
 

@@ -563,6 +563,9 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
     uint64_t* full = reinterpret_cast<uint64_t*>(base);
     uint64_t* done = full + kTileMaxNst;
     volatile int* abort_flag = reinterpret_cast<volatile int*>(base + 16 * kTileMaxNst);
+    // rows of the tile in each buffer, written by the producer before the load
+    // is armed (the compute warps read it after the load's barrier completes)
+    int* meta_rows = reinterpret_cast<int*>(base + 256);
     unsigned char* ring = base + kTileHdrXTma;              // 1024-byte aligned buffers of M lines
     const int NST = A.nst;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -592,9 +595,7 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
                 if (threadIdx.x == 0) { report_status(A.status, 1); *abort_flag = 1; }
                 return;
             }
-            i64 row0, rs;
-            int nrows, gi, u0, w;
-            tile_geom<R, true, M>(A, tile, row0, rs, nrows, gi, u0, w);
+            const int nrows = meta_rows[b];
             C* tb = reinterpret_cast<C*>(ring + (size_t)b * M * 128);
             C va[E], vb[E];
             if (ua < nrows) tile_row_fft<R, SG, E, Rs...>(va, tb + ua * M, lane, A.tw, t2, t3);
@@ -628,10 +629,17 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
 
     // ---- producer warp: bulk loads in, tensor stores out ----
     if (lane != 0) return;
+    auto issue = [&](i64 tj, int bj) {
+        i64 row0, rs;
+        int nrows, gi, u0, w;
+        tile_geom<R, true, M>(A, tj, row0, rs, nrows, gi, u0, w);
+        meta_rows[bj] = nrows;
+        tile_issue<R, true, M>(A, tj, reinterpret_cast<C*>(ring + (size_t)bj * M * 128), &full[bj]);
+    };
     uint32_t issued_par = 0;   // bit b: parity of the last load into buffer b
     for (int j = 0; j < NST; ++j) {
         const i64 tj = blockIdx.x + (i64)j * gridDim.x;
-        if (tj < A.ntiles) tile_issue<R, true, M>(A, tj, reinterpret_cast<C*>(ring + (size_t)j * M * 128), &full[j]);
+        if (tj < A.ntiles) issue(tj, j);
     }
     int b = 0;
     uint32_t par = 0;
@@ -654,7 +662,7 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
         bulk_wait_read_all();
         const i64 tn = tile + (i64)NST * gridDim.x;
         if (tn < A.ntiles) {
-            tile_issue<R, true, M>(A, tn, reinterpret_cast<C*>(ring + (size_t)b * M * 128), &full[b]);
+            issue(tn, b);
             issued_par = (issued_par & ~(1u << b)) | ((par ^ 1u) << b);
         }
         if (++b == NST) { b = 0; par ^= 1; }

@@ -188,7 +188,7 @@ def _tma_unswizzle_128b(offset):
     return offset ^ (((offset >> 7) & 7) << 4)
 
 
-@pytest.mark.parametrize("es,M", [(8, 256), (8, 512), (8, 768), (16, 256), (16, 512)])
+@pytest.mark.parametrize("es,M", [(8, 256), (8, 512), (16, 256), (16, 512)])
 def test_tensor_store_staging_matches_the_map_swizzle(es, M):
     """fft_tile_xpose_tma_kernel: compute warp w writes rows (2w, 2w+1) of
     point i into line i at chunk (pair ^ (i & 7)) (complex64: one 16-byte chunk
