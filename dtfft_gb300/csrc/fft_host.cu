@@ -1051,6 +1051,7 @@ struct XTma {
     std::vector<int> seg_group;    // group of each segment
     int nst = 0;
     size_t smem = 0;
+    int box_i = 256;               // points per tensor store: 256, 128, 64 or 32
     std::mutex mu;
     std::vector<std::pair<const void*, TmaXMaps*>> maps;   // per output pointer, most recent last
     ~XTma() { for (auto& e : maps) delete e.second; }
@@ -1060,13 +1061,13 @@ struct XTma {
 // an 8-point boundary (the 128-byte swizzle of the staged lines repeats every
 // 8 lines), no box reads past the tile's M lines, destination base and strides
 // are 16-byte multiples, and the maps fit the kernel parameter.
-static bool xtma_fits(int m, int es, const std::vector<FSeg>& segs) {
+static bool xtma_fits(int m, int es, const std::vector<FSeg>& segs, int box_i = 256) {
     if (segs.empty() || (int)segs.size() > kTmaXMaxSegs) return false;
     for (const FSeg& sg : segs) {
         const int len = sg.i1 - sg.i0;
         if (len < 1 || sg.i0 % 8) return false;
-        const int box = std::min(len, 256);
-        for (int i = sg.i0; i < sg.i1; i += 256)
+        const int box = std::min(len, box_i);
+        for (int i = sg.i0; i < sg.i1; i += box_i)
             if (i + box > m) return false;
         if ((sg.dst_off * es) % 16 || (sg.di * es) % 16 || (sg.dw * es) % 16) return false;
         if (sg.di * es >= (1LL << 40) || sg.dw * es >= (1LL << 40) || sg.di < 1 || sg.dw < 0) return false;
@@ -1092,7 +1093,7 @@ static dtfft_error_t xtma_encode(const XTma& x, int es, void* out, TmaXMaps* mp)
         cuuint64_t gdim[3] = {(cuuint64_t)g.nu * w8, (cuuint64_t)len, (cuuint64_t)std::max(g.nw, 1)};
         cuuint64_t gstr[2] = {(cuuint64_t)(sg.di * es), (cuuint64_t)(std::max<i64>(sg.dw, 1) * es)};
         if (g.nw <= 1) gstr[1] = gstr[0] * (cuuint64_t)len;   // a single w plane: any stride does
-        cuuint32_t box[3] = {16, (cuuint32_t)std::min(len, 256), 1};
+        cuuint32_t box[3] = {16, (cuuint32_t)std::min(len, x.box_i), 1};
         cuuint32_t estr[3] = {1, 1, 1};
         void* base = (char*)out + sg.dst_off * es;
         const CUresult r = enc(&mp->map[k], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, base, gdim, gstr, box, estr,
@@ -1320,6 +1321,7 @@ static dtfft_error_t launch_fused_tile_tma(int m, XTma& x, const void* tw, const
     typedef typename CT<R>::T C;
     TXArgs<R> X;
     TArgs<R>& P = X.a;
+    X.box_i = x.box_i;
     P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)tw;
     P.nsig = 0; P.groups = (const FGroup*)groups; P.segs = (const FSeg*)segs; P.ngroups = ngroups;
     P.ntiles = tiles; P.S = 128 / (int)sizeof(C); P.nst = x.nst; P.pair_ok = 0; P.wait_limit = g_wait_limit;
@@ -1395,8 +1397,16 @@ dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int i
     key << dev << "|" << m_ << "|" << dbl_ << "|" << S_ << "|" << ngroups_ << "|" << ctas_ << "|" << smem_;
     std::lock_guard<std::mutex> lk(g_ft_tune_mu);
     auto apply = [&](int c, int w) {
-        if (c < 0) {   // the tensor-store write-out
+        if (c < 0) {   // the tensor-store write-out, stores of 256 >> (-1 - c) points
             if (!xtma_) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+            const int box = 256 >> (-1 - c);
+            if (!xtma_fits(m_, dbl_ ? 16 : 8, xtma_->segs, box)) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+            std::lock_guard<std::mutex> lk2(xtma_->mu);
+            if (xtma_->box_i != box) {   // the cached maps hold the old box
+                for (auto& e : xtma_->maps) delete e.second;
+                xtma_->maps.clear();
+                xtma_->box_i = box;
+            }
             use_xtma_ = true;
             return DTFFT_SUCCESS;
         }
@@ -1423,7 +1433,8 @@ dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int i
         return DTFFT_SUCCESS;   // keep the default split when scratch is not available
     }
     cudaMemsetAsync(a, 0, bytes, s);
-    static const int cands[][2] = {{-1, -1}, {0, 0}, {3, 5}, {4, 4}, {2, 6}, {4, 8}, {6, 6}, {8, 4}};
+    static const int cands[][2] = {{-1, -1}, {-2, -1}, {-3, -1}, {-4, -1}, {0, 0}, {3, 5}, {4, 4},
+                                   {2, 6}, {4, 8}, {6, 6}, {8, 4}};
     int best_c = 0, best_w = 0;
     float best_ms = 1e30f;
     cudaEvent_t e0, e1;
@@ -1445,7 +1456,9 @@ dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int i
         cudaEventElapsedTime(&ms, e0, e1);
         ms /= (float)std::max(iters, 1);
         if (log) {
-            if (c[0] < 0) printf("dtFFT-gb300: fused pass m=%d tensor-store write-out: %.4f ms\n", m_, ms);
+            if (c[0] < 0)
+                printf("dtFFT-gb300: fused pass m=%d tensor-store write-out, %d-point stores: %.4f ms\n", m_,
+                       256 >> (-1 - c[0]), ms);
             else printf("dtFFT-gb300: fused pass m=%d warps %d+%d: %.4f ms\n", m_, c[0], c[1], ms);
         }
         if (ms < best_ms) { best_ms = ms; best_c = c[0]; best_w = c[1]; }

@@ -507,7 +507,9 @@ __global__ void __launch_bounds__(32 * (NCW + NSW), 1) fft_tile_xpose_kernel(TAr
 //  - one producer warp issues the bulk loads, and per destination segment
 //    the cp.async.bulk.tensor stores of the transposed lines (boxes of
 //    S rows x up to 256 points, the tensor map un-swizzles them), then reuses
-//    the buffer for the next load once the store has read it.
+//    the buffer for the next load once the store has read it.  The boxes'
+//    extent along the points (256, 128, 64 or 32) is a launch parameter that
+//    the autotuner chooses.
 // No thread of the SM executes a global store; each point leaves as part of a
 // 128-byte line of the destination rank's block.
 constexpr int kTmaXMaxSegs = 48;
@@ -520,6 +522,7 @@ struct TmaXMaps {
 template <typename R>
 struct TXArgs {
     TArgs<R> a;
+    int box_i;        // points per tensor store (the maps' box extent along i)
     TmaXMaps m;
 };
 
@@ -563,9 +566,6 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
     uint64_t* full = reinterpret_cast<uint64_t*>(base);
     uint64_t* done = full + kTileMaxNst;
     volatile int* abort_flag = reinterpret_cast<volatile int*>(base + 16 * kTileMaxNst);
-    // rows of the tile in each buffer, written by the producer before the load
-    // is armed (the compute warps read it after the load's barrier completes)
-    int* meta_rows = reinterpret_cast<int*>(base + 256);
     unsigned char* ring = base + kTileHdrXTma;              // 1024-byte aligned buffers of M lines
     const int NST = A.nst;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -595,7 +595,9 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
                 if (threadIdx.x == 0) { report_status(A.status, 1); *abort_flag = 1; }
                 return;
             }
-            const int nrows = meta_rows[b];
+            i64 row0, rs;
+            int nrows, gi, u0, w;
+            tile_geom<R, true, M>(A, tile, row0, rs, nrows, gi, u0, w);
             C* tb = reinterpret_cast<C*>(ring + (size_t)b * M * 128);
             C va[E], vb[E];
             if (ua < nrows) tile_row_fft<R, SG, E, Rs...>(va, tb + ua * M, lane, A.tw, t2, t3);
@@ -630,10 +632,6 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
     // ---- producer warp: bulk loads in, tensor stores out ----
     if (lane != 0) return;
     auto issue = [&](i64 tj, int bj) {
-        i64 row0, rs;
-        int nrows, gi, u0, w;
-        tile_geom<R, true, M>(A, tj, row0, rs, nrows, gi, u0, w);
-        meta_rows[bj] = nrows;
         tile_issue<R, true, M>(A, tj, reinterpret_cast<C*>(ring + (size_t)bj * M * 128), &full[bj]);
     };
     uint32_t issued_par = 0;   // bit b: parity of the last load into buffer b
@@ -654,7 +652,7 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
         for (int kk = 0; kk < g.nseg; ++kk) {
             const FSeg sg = A.segs[g.seg_first + kk];
             const CUtensorMap* map = &X.m.map[g.seg_first + kk];
-            for (int i = sg.i0; i < sg.i1; i += 256)
+            for (int i = sg.i0; i < sg.i1; i += X.box_i)
                 tma_store_3d(map, tb + (size_t)i * 128, u0 * (ES / 8), i - sg.i0, w);
         }
         bulk_commit();
