@@ -218,7 +218,8 @@ def _tune_records(dt):
         kinds[k] = kinds.get(k, 0) + 1
     gain = sorted(recs, key=lambda r: -(r["runner_up_ms"] - r["chosen_ms"]) if r["runner_up"] else 0)
     return {"steps_tuned": len(recs), "candidates_timed": sum(r["candidates"] for r in recs),
-            "chosen_kinds": kinds, "largest_margins": gain[:12]}
+            "chosen_kinds": kinds, "largest_margins": gain[:12],
+            "fused_passes": [r for r in recs if r["step"].startswith("fused")]}
 
 
 def batched_section(args, dt, dev, stream, peak):
@@ -804,6 +805,7 @@ def run_ours(args):
                                          "what": "the step's H2D and D2H copies alone, concurrently"}}
                     if e2e_ms else None),
             "gpu_launches": launches,
+            "autotune": _tune_records(dt) if args.effort == 3 else None,
             "cpu_baseline": cpu,
             "clocks": clk,
             "transpose_only": tonly,

@@ -1436,7 +1436,14 @@ dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int i
     static const int cands[][2] = {{-1, -1}, {-2, -1}, {-3, -1}, {-4, -1}, {0, 0}, {3, 5}, {4, 4},
                                    {2, 6}, {4, 8}, {6, 6}, {8, 4}};
     int best_c = 0, best_w = 0;
-    float best_ms = 1e30f;
+    float best_ms = 1e30f, second_ms = 1e30f;
+    std::string best_name, second_name;
+    int timed = 0;
+    auto cand_name = [](int c, int w) {
+        if (c < 0) return std::string("tensor_store:") + std::to_string(256 >> (-1 - c));
+        if (c == 0) return std::string("store_warps:default");
+        return std::string("store_warps:") + std::to_string(c) + "+" + std::to_string(w);
+    };
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1461,7 +1468,13 @@ dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int i
                        256 >> (-1 - c[0]), ms);
             else printf("dtFFT-gb300: fused pass m=%d warps %d+%d: %.4f ms\n", m_, c[0], c[1], ms);
         }
-        if (ms < best_ms) { best_ms = ms; best_c = c[0]; best_w = c[1]; }
+        ++timed;
+        if (ms < best_ms) {
+            second_ms = best_ms; second_name = best_name;
+            best_ms = ms; best_c = c[0]; best_w = c[1]; best_name = cand_name(c[0], c[1]);
+        } else if (ms < second_ms) {
+            second_ms = ms; second_name = cand_name(c[0], c[1]);
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1470,6 +1483,16 @@ dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int i
     cudaFree(b);
     cudaGetLastError();
     g_ft_tune[key.str()] = std::make_pair(best_c, best_w);
+    if (timed > 0) {
+        TuneRecord rec;
+        rec.step = std::string("fused_xpose_m") + std::to_string(m_) + (dbl_ ? "_f64" : "_f32") + "_tiles" +
+                   std::to_string(ctas_);
+        rec.best = best_name; rec.best_ms = best_ms;
+        if (second_ms < 1e29f) { rec.second = second_name; rec.second_ms = second_ms; }
+        rec.candidates = timed;
+        std::lock_guard<std::mutex> lk3(g_step_tune_mu);
+        g_tune_records.push_back(rec);
+    }
     return apply(best_c, best_w);
 }
 

@@ -317,11 +317,11 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
 // host side
 // ---------------------------------------------------------------------------
 
-struct TcKernel { int R1, R2; const void* fn; int smem; int tmem_cols; };
+struct TcKernel { int R1, R2; const void* fn; int smem; };
 
 template <int R1, int R2>
 static TcKernel tc_entry() {
-    return TcKernel{R1, R2, (const void*)fft_tc_kernel<R1, R2>, TcShape<R1, R2>::SMEM, TcShape<R1, R2>::TMEM_COLS};
+    return TcKernel{R1, R2, (const void*)fft_tc_kernel<R1, R2>, TcShape<R1, R2>::SMEM};
 }
 
 // row lengths with a tensor-core form: m = R1 * R2
@@ -403,17 +403,12 @@ dtfft_error_t tc_create(int m, void** out) {
             e = DTFFT_ERROR_GPU_CALL_FAILED;
     }
     if (e == DTFFT_SUCCESS) {
-        // shared memory over L1, so that several CTAs share an SM and one CTA's
-        // MMAs and waits overlap the others' operand preparation
         if (cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, k.smem) != cudaSuccess ||
-            cudaFuncSetAttribute(k.fn, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f->per_sm, k.fn, 128, k.smem) != cudaSuccess ||
             f->per_sm < 1)
             e = DTFFT_ERROR_GPU_CALL_FAILED;
-        // resident CTAs must fit the SM's 512 tensor-memory columns together,
-        // so that no CTA's allocation waits for another's
-        f->per_sm = std::max(1, std::min(f->per_sm, 512 / k.tmem_cols));
+        // each CTA holds up to 256 tensor-memory columns of the SM's 512
+        f->per_sm = std::min(f->per_sm, 2);
         int dev = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&f->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || f->sms < 1)
