@@ -228,7 +228,7 @@ def batched_section(args, dt, dev, stream, peak):
     transforms as tuned plans (EXHAUSTIVE: measured transpose tiles) replayed
     as one CUDA graph per direction (dtfft_gb_batch_execute)."""
     import torch
-    shapes = batch_shapes()
+    shapes = batch_shapes(count=args.batch_count)
     cfg = dt.Config(stream=stream.cuda_stream)
     plain, tuned, bufs = [], [], []
     pass_bytes = 0
@@ -310,6 +310,26 @@ def batched_section(args, dt, dev, stream, peak):
     bwd_nodes = batch.graph_nodes
     torch.cuda.synchronize()
     batch.destroy()
+    # forward spectra of the first C2C and the first R2C member, five Z-lines
+    # each against numpy FP64 (inputs regenerated from their seeds)
+    member_err = {}
+    for i in range(2):
+        kind, dims = shapes[i]
+        p = plain[i]
+        x, o, aux = bufs[i]
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(1000 + i)
+        n = p.alloc_size
+        if kind == "c2c":
+            x.copy_(torch.complex(torch.randn(n, device=dev, generator=gen), torch.randn(n, device=dev, generator=gen)))
+        else:
+            x.copy_(torch.randn(n, device=dev, generator=gen))
+        nx, ny, nz = dims
+        glob = x[:nx * ny * nz].cpu().numpy().reshape(nz, ny, nx)
+        p.execute(x, o, dt.Execute.FORWARD, aux)
+        torch.cuda.synchronize()
+        pts = _z_line_points(nx // 2 + 1 if kind == "r2c" else nx, ny)
+        member_err[f"{kind}_{nx}x{ny}x{nz}"] = _rel_l2(_device_z_lines(dt, p, o, pts, nz), _fp64_z_lines(glob, pts, kind))
     for p in plain + tuned:
         p.destroy()
     n_c2c = sum(1 for k, _ in shapes if k == "c2c")
@@ -321,6 +341,7 @@ def batched_section(args, dt, dev, stream, peak):
             "batched_graph": {"cycles_per_s": 1000.0 / batch_ms, "ms_per_cycle": batch_ms,
                               "graph_launches_per_cycle": 2, "graph_nodes_per_cycle": fwd_nodes + bwd_nodes},
             "speedup": seq_ms / batch_ms,
+            "fwd_rel_l2_vs_numpy_fp64_z_lines": member_err,
             "sequential_kernel_classes": kernel_classes,
             "unfused_pass_bytes_per_cycle": pass_bytes,
             "fft_autotune": tune,
@@ -328,12 +349,71 @@ def batched_section(args, dt, dev, stream, peak):
                               "batched_graph": pass_bytes / (batch_ms * 1e-3) / 1e12}}
 
 
+def _z_line_points(nx, ny):
+    """(kx, ky) of the sampled Z-lines: the zero and last frequencies, the
+    middle and two interior points."""
+    return [(0, 0), (nx - 1, ny - 1), (nx // 2, ny // 5), (11 % nx, 1 % ny), (nx // 3, ny - 1)]
+
+
+def _fp64_z_lines(g, pts, kind="c2c"):
+    """FP64 values along Z of the forward 3D transform of g (numpy, C order
+    [z][y][x]) at the fixed (kx, ky) frequencies `pts`, computed with numpy
+    as the contraction of g with the two basis vectors followed by the 1D
+    transform along Z (the transform is separable), reading g in chunks of
+    z-planes.  kind: "c2c" / "r2c" (exp(-2 pi i j k / n) along X and Y, FFT
+    along Z) or "dct2" (FFTW's REDFT10 2 cos(pi k (2j + 1) / (2n)) on every axis)."""
+    import numpy as np
+    nz, ny, nx = g.shape
+    kx = np.array([p[0] for p in pts])
+    ky = np.array([p[1] for p in pts])
+    if kind == "dct2":
+        bx = 2 * np.cos(np.pi * np.outer(2 * np.arange(nx) + 1, kx) / (2 * nx))
+        by = 2 * np.cos(np.pi * np.outer(2 * np.arange(ny) + 1, ky) / (2 * ny))
+        acc = np.zeros((len(pts), nz))
+    else:
+        bx = np.exp(-2j * np.pi * np.outer(np.arange(nx), kx) / nx)
+        by = np.exp(-2j * np.pi * np.outer(np.arange(ny), ky) / ny)
+        acc = np.zeros((len(pts), nz), dtype=np.complex128)
+    for z0 in range(0, nz, 16):
+        G = np.asarray(g[z0:z0 + 16], dtype=acc.dtype)
+        t = (G.reshape(-1, nx) @ bx).reshape(G.shape[0], ny, len(pts))
+        acc[:, z0:z0 + G.shape[0]] = np.einsum("zyk,yk->kz", t, by)
+    if kind == "dct2":
+        import scipy.fft as sf
+        return sf.dct(acc, type=2, axis=1, norm=None)
+    return np.fft.fft(acc, axis=1)
+
+
+def _device_z_lines(dt, plan, buf, pts, nz):
+    """The same Z-lines from a plan's forward output (Z pencils of every
+    virtual rank, packed; a rank's block stores (z, x, y) with z fastest),
+    located through the library's own per-rank pencils and offsets."""
+    import numpy as np
+    out = []
+    for kx, ky in pts:
+        for r in range(plan.nranks):
+            pen, off = plan.vrank_pencil(dt.Layout.Z_PENCILS, r)
+            sz, sx, sy = pen.starts
+            cz, cx, cy = pen.counts
+            if sx <= kx < sx + cx and sy <= ky < sy + cy:
+                base = off + cz * ((kx - sx) + cx * (ky - sy))
+                out.append(buf[base:base + cz].cpu().numpy().astype(np.complex128 if buf.is_complex() else np.float64))
+                break
+    return np.stack(out)
+
+
+def _rel_l2(a, b):
+    import numpy as np
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
 def tensor_core_section(args, dt, dev, stream, sizes=(768, 1024)):
     """C2C complex64 N^3 (one process, Z-slab plan), inputs uniform[-1,1) re/im
     plus 1e3-amplitude spikes at 0.1% of the points: FP32 Stockham row passes
     against the tensor-core form (DFT-matrix GEMMs on tcgen05, FP16 hi + lo,
-    FP32 accumulate), fwd+bwd cycles/s and forward error against an FP64
-    (complex128) plan of the same transform."""
+    FP32 accumulate), fwd+bwd cycles/s, forward error against an FP64
+    (complex128) plan of the same transform, and against numpy FP64 values of
+    five Z-lines of the spectrum."""
     import torch
     L = dt.lib()
     L.dtfft_gb_set_fft_form.argtypes = [ctypes.c_int32]
@@ -364,6 +444,8 @@ def tensor_core_section(args, dt, dev, stream, sizes=(768, 1024)):
         torch.cuda.synchronize()
         del a64, aux64
         ref_norm = float(torch.linalg.vector_norm(b64))
+        pts = _z_line_points(N, N)
+        lines_ref = _fp64_z_lines(x0.cpu().numpy().reshape(N, N, N), pts)
         a = torch.empty_like(x0)
         b = torch.empty_like(x0)
         aux = torch.empty_like(x0)
@@ -375,6 +457,7 @@ def tensor_core_section(args, dt, dev, stream, sizes=(768, 1024)):
             p.execute(a, b, dt.Execute.FORWARD, aux)
             torch.cuda.synchronize()
             err = float(torch.linalg.vector_norm(b.to(torch.complex128) - b64)) / ref_norm
+            err_lines = _rel_l2(_device_z_lines(dt, p, b, pts, N), lines_ref)
             p.execute(b, a, dt.Execute.BACKWARD, aux)
             torch.cuda.synchronize()
             rt = float(torch.linalg.vector_norm(a / n - x0) / torch.linalg.vector_norm(x0))
@@ -401,6 +484,7 @@ def tensor_core_section(args, dt, dev, stream, sizes=(768, 1024)):
             prof = sorted(_profile_results(L), key=lambda r: -r[2])
             rows = [r for r in prof if "rows_c2c" in r[0]]
             row[name] = {"cycles_per_s": 1000.0 / ms, "ms_per_cycle": ms, "fwd_rel_l2_vs_fp64": err,
+                         "fwd_rel_l2_vs_numpy_fp64_z_lines": err_lines,
                          "roundtrip_rel_l2": rt,
                          "row_pass_kernel": rows[0][0] if rows else None,
                          "row_pass_ms": rows[0][2] / max(rows[0][1], 1) if rows else None,
@@ -472,8 +556,9 @@ def config1_section(args, dt, dev, stream):
 def config3_section(args, dt, dev, stream):
     """3D R2C float64 1024x1024x512 (real input N(0,1)) on a 4x4 virtual grid,
     and the R2R plan of the same grid with DCT-II on every axis: fwd+bwd
-    cycles/s and the forward error of a spot check against an FP64 DFT of one
-    Z-line (the full FP64 oracle of a 4 GiB transform is the round trip)."""
+    cycles/s, the round trip, and the forward spectrum on five Z-lines against
+    numpy FP64."""
+    import numpy as np
     import torch
     dims = [1024, 1024, 512]
     comm = dt.cart_comm([1, 4, 4])
@@ -509,6 +594,24 @@ def config3_section(args, dt, dev, stream):
             plan.execute(a, b, dt.Execute.FORWARD, aux)
             plan.execute(b, a, dt.Execute.BACKWARD, aux)
 
+        # forward spectrum: five Z-lines against numpy FP64 (the global real
+        # array is assembled from every virtual rank's X pencil block)
+        plan.execute(a, b, dt.Execute.FORWARD, aux)
+        torch.cuda.synchronize()
+        gx = x0.cpu().numpy()
+        glob = np.empty((dims[2], dims[1], dims[0]))
+        for r in range(plan.nranks):
+            pen, off = plan.vrank_pencil(dt.Layout.X_PENCILS, r)
+            sx, sy, sz = pen.starts
+            cx, cy, cz = pen.counts
+            glob[sz:sz + cz, sy:sy + cy, sx:sx + cx] = gx[off:off + cx * cy * cz].reshape(cz, cy, cx)
+        del gx
+        nxo = dims[0] // 2 + 1 if kind == "r2c" else dims[0]
+        pts = _z_line_points(nxo, dims[1])
+        err_lines = _rel_l2(_device_z_lines(dt, plan, b, pts, dims[2]),
+                            _fp64_z_lines(glob, pts, "r2c" if kind == "r2c" else "dct2"))
+        del glob
+        a.copy_(x0)
         step()
         torch.cuda.synchronize()
         # unnormalised round trip: R2C scales by N, DCT-II/III by prod(2 n)
@@ -538,6 +641,7 @@ def config3_section(args, dt, dev, stream):
         flops = 2 * 2.5 * nreal * math.log2(nreal)
         big = max(n_in * 8, n_out * (16 if kind == "r2c" else 8))
         out[kind] = {"cycles_per_s": 1000.0 / ms, "ms_per_cycle": ms, "roundtrip_rel_l2": rt,
+                     "fwd_rel_l2_vs_numpy_fp64_z_lines": err_lines,
                      "fft_tflops_conventional": flops / (ms * 1e-3) / 1e12,
                      "frac_of_fp64_fma_peak": (flops / (ms * 1e-3) / 1e12) / fp64_peak if fp64_peak else None,
                      "kernels": [{"name": r[0], "launches": r[1], "total_ms": r[2],
@@ -591,6 +695,21 @@ def run_ours(args):
         plan.execute(a, b, dt.Execute.FORWARD, aux)
         plan.execute(b, a, dt.Execute.BACKWARD, aux)
 
+    # forward spectrum on five Z-lines against numpy FP64 (outside the timed region)
+    plan.execute(a, b, dt.Execute.FORWARD, aux)
+    torch.cuda.synchronize()
+    gx = x0.cpu().numpy()
+    glob = np.empty((DIMS[2], DIMS[1], DIMS[0]), dtype=np.complex64)
+    for r in range(plan.nranks):
+        pen, off = plan.vrank_pencil(dt.Layout.X_PENCILS, r)
+        sx, sy, sz = pen.starts
+        cx, cy, cz = pen.counts
+        glob[sz:sz + cz, sy:sy + cy, sx:sx + cx] = gx[off:off + cx * cy * cz].reshape(cz, cy, cx)
+    del gx
+    zpts = _z_line_points(DIMS[0], DIMS[1])
+    fwd_lines_err = _rel_l2(_device_z_lines(dt, plan, b, zpts, DIMS[2]), _fp64_z_lines(glob, zpts))
+    del glob
+    a.copy_(x0)
     # round-trip error (outside the timed region): fwd, bwd, scale
     step()
     torch.cuda.synchronize()
@@ -792,6 +911,7 @@ def run_ours(args):
             "pass_equivalent_tbs": {"value": eff_tbs, "what": "unfused pass count 2 x (3 FFT + 2 transposes) x "
                                     "2 B per cycle / time; fusion makes it exceed the DRAM traffic"},
             "roundtrip_rel_l2": rt,
+            "fwd_rel_l2_vs_numpy_fp64_z_lines": fwd_lines_err,
             "roofline": {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": _traffic_for(top[0]), "algorithmic_bytes": algo_bytes,
@@ -833,6 +953,8 @@ def main():
     ap.add_argument("--no-transpose-only", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-transform batched section")
     ap.add_argument("--no-tc", action="store_true", help="skip the tensor-core 768^3 / 1024^3 section")
+    ap.add_argument("--batch-count", type=int, default=64,
+                    help="transforms of the batch section (fewer for profiling; the workload is 64)")
     ap.add_argument("--tc-sizes", type=int, nargs="+", default=[768, 1024],
                     help="cube edges of the tensor-core section (smaller ones for profiling)")
     ap.add_argument("--no-configs", action="store_true",

@@ -24,3 +24,25 @@ def test_reference_arm_json_line():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_bench_fp64_z_lines_equal_full_transforms():
+    """The bench's numpy FP64 Z-line check equals the full FP64 transforms."""
+    import numpy as np
+    import scipy.fft as sf
+    import bench
+    rng = np.random.default_rng(3)
+    g = rng.standard_normal((10, 12, 14)) + 1j * rng.standard_normal((10, 12, 14))
+    pts = bench._z_line_points(14, 12)
+    full = np.fft.fftn(g)
+    np.testing.assert_allclose(bench._fp64_z_lines(g, pts), np.stack([full[:, ky, kx] for kx, ky in pts]),
+                               atol=1e-10)
+    r = rng.standard_normal((10, 12, 14))
+    full = np.fft.rfftn(r)
+    pts = bench._z_line_points(8, 12)
+    np.testing.assert_allclose(bench._fp64_z_lines(r, pts, "r2c"), np.stack([full[:, ky, kx] for kx, ky in pts]),
+                               atol=1e-10)
+    full = sf.dctn(r, type=2, norm=None)
+    pts = bench._z_line_points(14, 12)
+    np.testing.assert_allclose(bench._fp64_z_lines(r, pts, "dct2"), np.stack([full[:, ky, kx] for kx, ky in pts]),
+                               atol=1e-9)
