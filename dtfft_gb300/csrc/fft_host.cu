@@ -355,6 +355,8 @@ static dtfft_error_t prepare_launch(const FftStep& S) {
     return set_smem_attrs(fn, S.smem);
 }
 
+static dtfft_error_t upload_mode_tables(FftStep& S, std::vector<void*>& owned);
+
 static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
     // DCT/DST-II and -III of even length through an n/2-point complex FFT when
     // the register kernel has a schedule for n/2 (half the arithmetic)
@@ -387,10 +389,12 @@ static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
         }
     } else if (!make_schedule(m, S.sched)) {
         // a prime factor above the direct butterflies: Bluestein's chirp-z form
-        const int kind = S.mode == M_C2C ? 0 : S.mode == M_R2C_FULL ? 1 : S.mode == M_C2R_FULL ? 2 : -1;
+        const bool r2r = S.mode >= M_DCT1 && S.mode <= M_DST4;
+        const int kind = S.mode == M_C2C ? 0 : S.mode == M_R2C_FULL ? 1 : S.mode == M_C2R_FULL ? 2 : r2r ? 3 : -1;
         if (kind < 0) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+        if (r2r) GB_TRY(upload_mode_tables(S, owned));
         return blue_create(S.dbl, m, sign, kind, S.nsig, S.idist, S.odist, S.plane, S.ld, S.ncols, S.cols ? 1 : 0,
-                           &S.blue);
+                           &S.blue, S.mode, S.n, S.ta, S.tb);
     }
     if (fft_form() == 1 && !S.cols && !S.dbl && S.mode == M_C2C && S.idist == m && S.odist == m && tc_supported(m))
         GB_TRY(tc_create(m, &S.tc));
@@ -437,6 +441,13 @@ tables:
     // tables
     std::vector<double> tw = table_exp(m, 1, m);
     GB_TRY(upload_table(tw, S.dbl, owned, &S.tw));
+    GB_TRY(upload_mode_tables(S, owned));
+    return prepare_launch(S);
+}
+
+// Pre/post-processing tables of the step's mode (S.ta, S.tb).
+static dtfft_error_t upload_mode_tables(FftStep& S, std::vector<void*>& owned) {
+    const int m = S.m;
     switch (S.mode) {
     case M_R2C_HALF: GB_TRY(upload_table(table_exp(m + 1, 1, S.n), S.dbl, owned, &S.ta)); break;
     case M_C2R_HALF: GB_TRY(upload_table(table_exp(m, 1, S.n), S.dbl, owned, &S.ta)); break;
@@ -462,7 +473,7 @@ tables:
     } break;
     default: break;
     }
-    return prepare_launch(S);
+    return DTFFT_SUCCESS;
 }
 
 template <typename R, bool FUSED>
@@ -1049,6 +1060,11 @@ struct XTma {
     std::vector<FGroup> groups;
     std::vector<FSeg> segs;
     std::vector<int> seg_group;    // group of each segment
+    int S = 0;                     // rows per tile: a point's line is S * sizeof(complex) bytes
+    int lb = 0;                    // line bytes: 128 or 64 (the tensor maps' swizzle span)
+    int ncw = 0;                   // compute warps
+    const void* dgroups = nullptr; // device groups tiled by S (nullptr: the pass's own groups)
+    i64 tiles = 0;                 // tiles of the pass at S rows
     int nst = 0;
     size_t smem = 0;
     int box_i = 256;               // points per tensor store: 256, 128, 64 or 32
@@ -1059,8 +1075,9 @@ struct XTma {
 
 // Every store box of the pass fits the tensor-store kernel: segments start on
 // an 8-point boundary (the 128-byte swizzle of the staged lines repeats every
-// 8 lines), no box reads past the tile's M lines, destination base and strides
-// are 16-byte multiples, and the maps fit the kernel parameter.
+// 8 lines, the 64-byte one every 8 lines of 64 bytes), no box reads past the
+// tile's M lines, destination base and strides are 16-byte multiples, and the
+// maps fit the kernel parameter.
 static bool xtma_fits(int m, int es, const std::vector<FSeg>& segs, int box_i = 256) {
     if (segs.empty() || (int)segs.size() > kTmaXMaxSegs) return false;
     for (const FSeg& sg : segs) {
@@ -1076,8 +1093,8 @@ static bool xtma_fits(int m, int es, const std::vector<FSeg>& segs, int box_i = 
 }
 
 // Tensor maps of every destination segment of the pass for output `out`:
-// (u in 8-byte words, i, w) of the segment's block, boxes of one 128-byte
-// line (u) by up to 256 points, 128-byte swizzle.
+// (u in 8-byte words, i, w) of the segment's block, boxes of one line (u, 128
+// or 64 bytes) by up to 256 points, swizzled over the line's span.
 static dtfft_error_t xtma_encode(const XTma& x, int es, void* out, TmaXMaps* mp) {
     typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -1093,11 +1110,12 @@ static dtfft_error_t xtma_encode(const XTma& x, int es, void* out, TmaXMaps* mp)
         cuuint64_t gdim[3] = {(cuuint64_t)g.nu * w8, (cuuint64_t)len, (cuuint64_t)std::max(g.nw, 1)};
         cuuint64_t gstr[2] = {(cuuint64_t)(sg.di * es), (cuuint64_t)(std::max<i64>(sg.dw, 1) * es)};
         if (g.nw <= 1) gstr[1] = gstr[0] * (cuuint64_t)len;   // a single w plane: any stride does
-        cuuint32_t box[3] = {16, (cuuint32_t)std::min(len, x.box_i), 1};
+        cuuint32_t box[3] = {(cuuint32_t)(x.lb / 8), (cuuint32_t)std::min(len, x.box_i), 1};
         cuuint32_t estr[3] = {1, 1, 1};
         void* base = (char*)out + sg.dst_off * es;
         const CUresult r = enc(&mp->map[k], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, base, gdim, gstr, box, estr,
-                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE,
+                               x.lb == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                                CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return DTFFT_ERROR_GPU_CALL_FAILED;
     }
@@ -1203,26 +1221,54 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
                                  : TilePtr<float>::get(m, sg, true, p->ncw_, p->nsw_);
             err = set_smem_attrs(fn, ts.smem);
         }
-        // the tensor-store write-out when the pass's tiles are whole 128-byte
-        // lines and every segment fits it (the default then)
-        const void* fk = dbl ? TilePtr<double>::get_tma(m, -1) : TilePtr<float>::get_tma(m, -1);
+        // the tensor-store write-out when a kernel is compiled for m, the
+        // tiles come out as whole 128- or 64-byte lines and every segment fits
+        // it (the default then); its tiles may hold fewer rows than the
+        // store-warp kernel's, over their own copy of the groups
+        int xs = 0, xw = 0;
+        const void* fk = dbl ? TilePtr<double>::get_tma(m, -1, &xs, &xw) : TilePtr<float>::get_tma(m, -1, &xs, &xw);
         const void* bk = dbl ? TilePtr<double>::get_tma(m, 1) : TilePtr<float>::get_tma(m, 1);
-        if (err == DTFFT_SUCCESS && fk && bk && ts.S * (int)es == 128 && tma_encode_tiled_fn() &&
-            xtma_fits(m, (int)es, segs)) {
+        // (the widest store box that keeps every box inside the tile's M lines)
+        int box = 256;
+        while (box > 32 && !xtma_fits(m, (int)es, segs, box)) box >>= 1;
+        if (err == DTFFT_SUCCESS && fk && bk && xs <= ts.S && (xs * (int)es == 128 || xs * (int)es == 64) &&
+            tma_encode_tiled_fn() && xtma_fits(m, (int)es, segs, box)) {
             XTma* x = new XTma();
+            x->box_i = box;
+            x->S = xs;
+            x->lb = xs * (int)es;
+            x->ncw = xw;
             x->groups = groups;
             x->segs = segs;
+            x->tiles = ctas;
+            if (xs != ts.S) {
+                x->tiles = 0;
+                for (FGroup& g : x->groups) {
+                    g.tiles_u = (g.nu + xs - 1) / xs;
+                    g.cta_begin = x->tiles;
+                    x->tiles += (i64)g.tiles_u * g.nw;
+                }
+            }
             for (size_t gi = 0; gi < groups.size(); ++gi)
                 for (int k = 0; k < groups[gi].nseg; ++k) x->seg_group.push_back((int)gi);
-            const size_t line_bytes = (size_t)m * 128;
+            const size_t line_bytes = (size_t)m * x->lb;
             x->nst = (int)std::min<size_t>(kTileMaxNst, (max_optin_smem() - 2 * kTileHdrXTma) / line_bytes);
             x->smem = 2 * kTileHdrXTma + (size_t)x->nst * line_bytes;
             // the driver validates the maps' shapes and strides when they are
             // encoded: try once on an aligned stand-in address (host only)
             TmaXMaps probe;
             const bool encodable = xtma_encode(*x, (int)es, (void*)(uintptr_t)4096, &probe) == DTFFT_SUCCESS;
-            if (encodable && x->nst >= 2 && set_smem_attrs(fk, x->smem) == DTFFT_SUCCESS &&
-                set_smem_attrs(bk, x->smem) == DTFFT_SUCCESS) {
+            bool ok = encodable && x->nst >= 2 && x->tiles <= 0x7fffffffLL &&
+                      set_smem_attrs(fk, x->smem) == DTFFT_SUCCESS && set_smem_attrs(bk, x->smem) == DTFFT_SUCCESS;
+            if (ok && xs != ts.S) {
+                void* dg = nullptr;
+                ok = cudaMalloc(&dg, sizeof(FGroup) * x->groups.size()) == cudaSuccess &&
+                     cudaMemcpy(dg, x->groups.data(), sizeof(FGroup) * x->groups.size(), cudaMemcpyHostToDevice) ==
+                         cudaSuccess;
+                if (dg) p->owned_.push_back(dg);
+                x->dgroups = dg;
+            }
+            if (ok) {
                 p->xtma_ = x;
                 p->use_xtma_ = true;
             } else {
@@ -1324,7 +1370,8 @@ static dtfft_error_t launch_fused_tile_tma(int m, XTma& x, const void* tw, const
     X.box_i = x.box_i;
     P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)tw;
     P.nsig = 0; P.groups = (const FGroup*)groups; P.segs = (const FSeg*)segs; P.ngroups = ngroups;
-    P.ntiles = tiles; P.S = 128 / (int)sizeof(C); P.nst = x.nst; P.pair_ok = 0; P.wait_limit = g_wait_limit;
+    if (x.dgroups) { P.groups = (const FGroup*)x.dgroups; tiles = x.tiles; }
+    P.ntiles = tiles; P.S = x.S; P.nst = x.nst; P.pair_ok = 0; P.wait_limit = g_wait_limit;
     P.status = status_ptr();
     {
         std::lock_guard<std::mutex> lk(x.mu);
@@ -1343,7 +1390,7 @@ static dtfft_error_t launch_fused_tile_tma(int m, XTma& x, const void* tw, const
     void (*kfn)(TXArgs<R>) = (void (*)(TXArgs<R>))TilePtr<R>::get_tma(m, sign);
     if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     const i64 grid = std::min<i64>(tiles, (i64)sm_count());
-    const int threads = 32 * (128 / (int)sizeof(C) / 2 + 1);
+    const int threads = 32 * (x.ncw + 1);
     void* tok = prof_begin(s);
     kfn<<<(unsigned)grid, threads, x.smem, s>>>(X);
     if (tok) prof_end(tok, std::string("ffttile_xtma_m") + std::to_string(m) + (sizeof(R) == 8 ? "_f64" : "_f32"), s);

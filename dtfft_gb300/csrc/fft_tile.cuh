@@ -547,15 +547,27 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 __device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
-template <typename R, int SG, int NCW, int E, int... Rs>
+// Byte offset, inside a point's line of LB bytes, of the 16-byte chunk `chunk`
+// under the tensor map's swizzle: 128-byte lines (SWIZZLE_128B) XOR the chunk
+// index with i mod 8, 64-byte lines (SWIZZLE_64B) with (i / 2) mod 4 - the
+// byte-address bits 7..9 (7..8) of line i in a 1024-byte aligned buffer.
+template <int LB>
+__device__ __forceinline__ int line_chunk(int i, int chunk) {
+    if constexpr (LB == 128) return (chunk ^ (i & 7)) << 4;
+    else return (chunk ^ ((i >> 1) & 3)) << 4;
+}
+
+template <typename R, int SG, int NCW, int RPW, int E, int... Rs>
 __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(const __grid_constant__ TXArgs<R> X) {
     typedef typename CT<R>::T C;
     constexpr int M = (Rs * ... * 1);
     constexpr int ES = (int)sizeof(C);
-    constexpr int S = 128 / ES;                 // rows per tile: one 128-byte line per point
+    constexpr int S = NCW * RPW;                // rows per tile
+    constexpr int LB = S * ES;                  // bytes of one point's line
     static_assert(M == E * 32, "one warp per row");
     static_assert(M % 16 == 0, "swizzles need 16-point blocks");
-    static_assert(2 * NCW == S, "one row pair per compute warp");
+    static_assert(RPW == 1 || RPW == 2, "one row or a row pair per compute warp");
+    static_assert(LB == 64 || LB == 128, "lines of 64 or 128 bytes");
     const TArgs<R>& A = X.a;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // full[b]: the load into buffer b landed; done[b]: the compute warps wrote
@@ -581,12 +593,12 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
     __syncthreads();
 
     if (warp < NCW) {
-        // ---- compute warps: rows 2*warp and 2*warp + 1 of every tile ----
+        // ---- compute warps: rows RPW*warp .. RPW*warp + RPW - 1 of every tile ----
         Tw2<R, E, Rs...> t2;
         t2.load(lane, A.tw);
         Tw3<R, E, Rs...> t3;
         t3.load(lane, A.tw);
-        const int ua = 2 * warp;
+        const int ua = RPW * warp;
         int b = 0;
         uint32_t par = 0;
         for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
@@ -598,26 +610,30 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
             i64 row0, rs;
             int nrows, gi, u0, w;
             tile_geom<R, true, M>(A, tile, row0, rs, nrows, gi, u0, w);
-            C* tb = reinterpret_cast<C*>(ring + (size_t)b * M * 128);
-            C va[E], vb[E];
+            C* tb = reinterpret_cast<C*>(ring + (size_t)b * M * LB);
+            C va[E], vb[RPW == 2 ? E : 1];
             if (ua < nrows) tile_row_fft<R, SG, E, Rs...>(va, tb + ua * M, lane, A.tw, t2, t3);
-            if (ua + 1 < nrows) tile_row_fft<R, SG, E, Rs...>(vb, tb + (ua + 1) * M, lane, A.tw, t2, t3);
+            if constexpr (RPW == 2)
+                if (ua + 1 < nrows) tile_row_fft<R, SG, E, Rs...>(vb, tb + (ua + 1) * M, lane, A.tw, t2, t3);
             // every row of the tile has been read: the buffer takes the transposed lines
             bar_sync_n(2, 32 * NCW);
             unsigned char* lines = reinterpret_cast<unsigned char*>(tb);
 #pragma unroll
             for (int q = 0; q < E; ++q) {
                 const int i = lane + 32 * q;
-                unsigned char* line = lines + (size_t)i * 128;
-                if constexpr (ES == 8) {
+                unsigned char* line = lines + (size_t)i * LB;
+                if constexpr (ES == 8 && RPW == 2) {
                     // rows ua, ua + 1 share the 16-byte chunk `warp`
                     float4 v;
                     v.x = va[q].x; v.y = va[q].y; v.z = vb[q].x; v.w = vb[q].y;
-                    *reinterpret_cast<float4*>(line + ((warp ^ (i & 7)) << 4)) = v;
+                    *reinterpret_cast<float4*>(line + line_chunk<LB>(i, warp)) = v;
+                } else if constexpr (ES == 8) {
+                    // row ua is half of the 16-byte chunk ua / 2
+                    *reinterpret_cast<C*>(line + line_chunk<LB>(i, ua >> 1) + 8 * (ua & 1)) = va[q];
                 } else {
                     // one 16-byte chunk per row
-                    *reinterpret_cast<C*>(line + ((ua ^ (i & 7)) << 4)) = va[q];
-                    *reinterpret_cast<C*>(line + (((ua + 1) ^ (i & 7)) << 4)) = vb[q];
+                    *reinterpret_cast<C*>(line + line_chunk<LB>(i, ua)) = va[q];
+                    if constexpr (RPW == 2) *reinterpret_cast<C*>(line + line_chunk<LB>(i, ua + 1)) = vb[q];
                 }
             }
             // the tensor stores read the buffer through the async proxy
@@ -632,7 +648,7 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
     // ---- producer warp: bulk loads in, tensor stores out ----
     if (lane != 0) return;
     auto issue = [&](i64 tj, int bj) {
-        tile_issue<R, true, M>(A, tj, reinterpret_cast<C*>(ring + (size_t)bj * M * 128), &full[bj]);
+        tile_issue<R, true, M>(A, tj, reinterpret_cast<C*>(ring + (size_t)bj * M * LB), &full[bj]);
     };
     uint32_t issued_par = 0;   // bit b: parity of the last load into buffer b
     for (int j = 0; j < NST; ++j) {
@@ -647,13 +663,13 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
         i64 row0, rs;
         int nrows, gi, u0, w;
         tile_geom<R, true, M>(A, tile, row0, rs, nrows, gi, u0, w);
-        const unsigned char* tb = ring + (size_t)b * M * 128;
+        const unsigned char* tb = ring + (size_t)b * M * LB;
         const FGroup& g = A.groups[gi];
         for (int kk = 0; kk < g.nseg; ++kk) {
             const FSeg sg = A.segs[g.seg_first + kk];
             const CUtensorMap* map = &X.m.map[g.seg_first + kk];
             for (int i = sg.i0; i < sg.i1; i += X.box_i)
-                tma_store_3d(map, tb + (size_t)i * 128, u0 * (ES / 8), i - sg.i0, w);
+                tma_store_3d(map, tb + (size_t)i * LB, u0 * (ES / 8), i - sg.i0, w);
         }
         bulk_commit();
         // the store has read the buffer: refill it
@@ -684,8 +700,9 @@ struct TilePtr {
     static void* get(int M, int sign, bool xpose, int ncw = 0, int nsw = 0);
     static int points_per_thread(int M);   // E of the compiled variants, 0 if none
     static int default_threads(int M, bool xpose);
-    // fused kernel with tensor-store write-out (fft_tile_xpose_tma_kernel), nullptr if none for M
-    static void* get_tma(int M, int sign);
+    // fused kernel with tensor-store write-out (fft_tile_xpose_tma_kernel), nullptr if none for M;
+    // *rows: rows per tile (one line of rows * sizeof(complex) bytes per point), *warps: compute warps
+    static void* get_tma(int M, int sign, int* rows = nullptr, int* warps = nullptr);
 };
 
 }  // namespace gb

@@ -40,22 +40,27 @@ void* TilePtr<float>::get(int M, int sign, bool xpose, int ncw, int nsw) {
 #undef GB_PLAIN
 #undef GB_XPOSE
 
-// Fused passes with the tensor-store write-out: 8 compute warps (one row
-// pair each of a 16-row tile) + 1 producer warp.  768-point rows keep the
-// store-warp kernel: two 768-point spectra per thread exceed the 168
-// registers of a 288-thread CTA (measured 1.75 vs 1.49 ms per 768^3 pass).
+// Fused passes with the tensor-store write-out, 8 compute warps + 1 producer
+// warp: 256- and 512-point rows as 16-row tiles (a row pair per warp, 128-byte
+// lines), 768- and 1024-point rows as 8-row tiles (a row per warp, 64-byte
+// lines: two 768-point spectra per thread exceed the 168 registers of a
+// 288-thread CTA).
+#define GB_TMA(RPW_, E_, ...)                                                                    \
+    if (rows) *rows = 8 * RPW_;                                                                  \
+    if (warps) *warps = 8;                                                                       \
+    return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<float, -1, 8, RPW_, E_, __VA_ARGS__>      \
+                    : (void*)fft_tile_xpose_tma_kernel<float, 1, 8, RPW_, E_, __VA_ARGS__>;
 template <>
-void* TilePtr<float>::get_tma(int M, int sign) {
+void* TilePtr<float>::get_tma(int M, int sign, int* rows, int* warps) {
     switch (M) {
-    case 256:
-        return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<float, -1, 8, 8, 8, 8, 4>
-                        : (void*)fft_tile_xpose_tma_kernel<float, 1, 8, 8, 8, 8, 4>;
-    case 512:
-        return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<float, -1, 8, 16, 16, 16, 2>
-                        : (void*)fft_tile_xpose_tma_kernel<float, 1, 8, 16, 16, 16, 2>;
+    case 256: GB_TMA(2, 8, 8, 8, 4)
+    case 512: GB_TMA(2, 16, 16, 16, 2)
+    case 768: GB_TMA(1, 24, 8, 8, 4, 3)
+    case 1024: GB_TMA(1, 32, 16, 16, 4)
     }
     return nullptr;
 }
+#undef GB_TMA
 
 template <>
 int TilePtr<float>::points_per_thread(int M) {

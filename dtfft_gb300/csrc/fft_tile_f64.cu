@@ -23,16 +23,18 @@ void* TilePtr<double>::get(int M, int sign, bool xpose, int ncw, int nsw) {
 }
 
 // Fused passes with the tensor-store write-out: 4 compute warps (one row
-// pair each of an 8-row tile) + 1 producer warp.
+// pair each of an 8-row tile, 128-byte lines) + 1 producer warp.
 template <>
-void* TilePtr<double>::get_tma(int M, int sign) {
+void* TilePtr<double>::get_tma(int M, int sign, int* rows, int* warps) {
+    if (rows) *rows = 8;
+    if (warps) *warps = 4;
     switch (M) {
     case 256:
-        return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<double, -1, 4, 8, 8, 8, 4>
-                        : (void*)fft_tile_xpose_tma_kernel<double, 1, 4, 8, 8, 8, 4>;
+        return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<double, -1, 4, 2, 8, 8, 8, 4>
+                        : (void*)fft_tile_xpose_tma_kernel<double, 1, 4, 2, 8, 8, 8, 4>;
     case 512:
-        return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<double, -1, 4, 16, 16, 16, 2>
-                        : (void*)fft_tile_xpose_tma_kernel<double, 1, 4, 16, 16, 16, 2>;
+        return sign < 0 ? (void*)fft_tile_xpose_tma_kernel<double, -1, 4, 2, 16, 16, 16, 2>
+                        : (void*)fft_tile_xpose_tma_kernel<double, 1, 4, 2, 16, 16, 16, 2>;
     }
     return nullptr;
 }

@@ -155,6 +155,53 @@ def test_tile_schedules(dt, orc, cuda, dims, grid, np_dtype, inplace):
     plan.destroy()
 
 
+def _profiled_names(L):
+    L.dtfft_gb_profile_count.restype = ctypes.c_int32
+    names = []
+    for i in range(L.dtfft_gb_profile_count()):
+        buf = ctypes.create_string_buffer(128)
+        n, ms = ctypes.c_int64(), ctypes.c_double()
+        L.dtfft_gb_profile_get(i, buf, 128, ctypes.byref(n), ctypes.byref(ms))
+        names.append(buf.value.decode())
+    return names
+
+
+@pytest.mark.parametrize("dims,grid", [
+    ([768, 84, 60], [1, 2, 1]),     # 5040 X rows: 16-row store-warp tiles, 8-row tensor-store tiles; 42 rows per rank
+    ([768, 64, 40], [1, 2, 1]),     # 2560 X rows: both kernels tile by 8
+    ([1024, 52, 48], [1, 2, 1]),    # 26 rows per rank: a ragged last tile of 2 rows
+    ([512, 84, 60], [1, 2, 1]),     # 128-byte lines of 16-row tiles, ragged (42 rows per rank)
+])
+def test_tensor_store_fused_pass(dt, orc, cuda, monkeypatch, dims, grid):
+    """The fused X pass with the tensor-store write-out (64-byte lines of
+    8-row tiles for 768- and 1024-point rows, 128-byte lines of 16-row tiles
+    for 512): the profiled launch list shows the kernel, and forward and
+    backward match the oracle."""
+    monkeypatch.setenv("DTFFT_GB_FUSE", "1")
+    L = dt.lib()
+    plan = dt.PlanC2C(dims, comm=comm_for(dt, grid), precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT,
+                      config=dt.Config(enable_z_slab=False))
+    dt.set_config(dt.Config())
+    g = random_global(tuple(dims[::-1]), np.complex64, seed=23)
+    x = orc.global_to_packed(g, 3, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, np.complex64, cuda)
+    c = empty(plan.alloc_size, np.complex64, cuda)
+    expect = orc.global_to_packed(orc.forward_values(g, "c2c"), 3, grid, _final_layout(plan, 3))
+    L.dtfft_gb_profile_start()
+    plan.execute(a, b, dt.Execute.FORWARD)
+    fwd = from_dev(b, expect.size, np.complex64)       # backward may overwrite its input
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    L.dtfft_gb_profile_stop()
+    names = _profiled_names(L)
+    assert ("ffttile_xtma_m%d_f32" % dims[0]) in names, names
+    assert L.dtfft_gb_device_status(1) == 0
+    assert orc.rel_l2(fwd, expect) <= TOL[np.complex64]
+    back = from_dev(c, x.size, np.complex64).astype(np.complex128) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= TOL[np.complex64]
+    plan.destroy()
+
+
 @pytest.mark.parametrize("dims,grid,np_dtype", [
     ([512, 64, 32], [1, 2, 2], np.complex64),
     ([256, 48, 256], [1, 1, 2], np.complex128),
@@ -469,6 +516,37 @@ def test_r2c_bluestein_lengths(dt, orc, cuda, dims, grid, np_dtype):
     c = empty(plan.alloc_size, np_dtype, cuda)
     plan.execute(b, c, dt.Execute.BACKWARD)
     back = from_dev(c, x.size, np_dtype) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= TOL[np_dtype]
+    plan.destroy()
+
+
+@pytest.mark.parametrize("dims,grid,kinds,np_dtype", [
+    ([132, 12, 10], [1, 1, 1], (3, 4, 5), np.float64),     # DCT-I: core 2(n-1) = 2 x 131
+    ([130, 10, 12], [1, 1, 1], (7, 8, 9), np.float64),     # DST-I: core 2(n+1) = 2 x 131
+    ([131, 12, 10], [1, 1, 1], (4, 5, 6), np.float32),     # DCT-II of prime length 131
+    ([10, 131, 12], [1, 1, 1], (8, 9, 10), np.float64),    # DST-II along columns (Y of the Z-slab pass)
+    ([12, 10, 139], [1, 2, 2], (5, 6, 9), np.float64),     # DST-III on Z of a 2x2 grid
+    ([131, 8], [1, 1], (6, 10), np.float32),               # DCT-IV: core 2n = 262
+    ([8, 131], [1, 1], (3, 10), np.float64),               # DST-IV on Y
+    ([262, 8], [1, 1], (5, 4), np.float64),                # even DCT-III whose half length (131) has no schedule
+    ([20, 131, 18], [1, 2, 2], (4, 9, 6), np.float64),
+])
+def test_r2r_bluestein_lengths(dt, orc, cuda, dims, grid, kinds, np_dtype):
+    """R2R kinds whose complex core length has a prime factor above 127 run
+    the core through Bluestein's chirp-z form (the reference's VkFFT and FFTW
+    executors take every length)."""
+    nd = len(dims)
+    plan = dt.PlanR2R(dims, kinds=list(kinds), comm=comm_for(dt, grid), precision=_prec(dt, np_dtype),
+                      executor=dt.Executor.VKFFT)
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=41, dist="normal")
+    x = orc.global_to_packed(g, nd, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(a, b, dt.Execute.FORWARD)
+    expect = orc.global_to_packed(orc.forward_values(g, "r2r", kinds=list(kinds)), nd, grid, _final_layout(plan, nd))
+    assert orc.rel_l2(from_dev(b, expect.size, np_dtype), expect) <= TOL[np_dtype]
+    plan.execute(b, a, dt.Execute.BACKWARD)
+    back = from_dev(a, x.size, np_dtype).astype(np.float64) / orc.r2r_roundtrip_scale(dims, kinds)
     assert orc.rel_l2(back, x) <= TOL[np_dtype]
     plan.destroy()
 

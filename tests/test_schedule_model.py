@@ -181,40 +181,55 @@ def test_tma_transpose_tile_coverage(ES):
             assert all(0 <= x and x + 16 <= 4 * TB * 128 for x in r)
 
 
-def _tma_unswizzle_128b(offset):
-    """Byte offset inside a 1024-byte aligned staging buffer that the 128-byte
-    tensor-map swizzle reads for logical byte `offset` of the box: the 16-byte
-    chunk index (bits 4..6) is XORed with the 128-byte line index mod 8 (bits 7..9)."""
-    return offset ^ (((offset >> 7) & 7) << 4)
+def _tma_unswizzle(offset, lb):
+    """Byte offset inside a 1024-byte aligned staging buffer that the tensor-map
+    swizzle of an lb-byte span reads for logical byte `offset` of the box: the
+    16-byte chunk index (bits 4..6 for 128 bytes, 4..5 for 64) is XORed with
+    address bits 7..9 (7..8)."""
+    if lb == 128:
+        return offset ^ (((offset >> 7) & 7) << 4)
+    return offset ^ (((offset >> 7) & 3) << 4)
 
 
-@pytest.mark.parametrize("es,M", [(8, 256), (8, 512), (16, 256), (16, 512)])
-def test_tensor_store_staging_matches_the_map_swizzle(es, M):
-    """fft_tile_xpose_tma_kernel: compute warp w writes rows (2w, 2w+1) of
-    point i into line i at chunk (pair ^ (i & 7)) (complex64: one 16-byte chunk
-    per row pair; complex128: one chunk per row).  The tensor store of a box of
-    lines [i0, i0 + L) with i0 % 8 == 0, read through the 128-byte swizzle, must
-    deliver element (u, i) of the destination block from where row u's value of
-    point i was written, for every (u, i), each staging byte used once."""
-    S = 128 // es
-    ncw = S // 2
+@pytest.mark.parametrize("es,M,rpw", [(8, 256, 2), (8, 512, 2), (16, 256, 2), (16, 512, 2), (8, 768, 1), (8, 1024, 1)])
+def test_tensor_store_staging_matches_the_map_swizzle(es, M, rpw):
+    """fft_tile_xpose_tma_kernel: compute warp w owns rows rpw*w .. rpw*w + rpw - 1
+    of an S-row tile (S = 8 * rpw for complex64, 4 * rpw for complex128) and
+    writes point i of them into line i (S * es bytes) at 16-byte chunk
+    c ^ (i & 7) (128-byte lines) or c ^ ((i >> 1) & 3) (64-byte lines), where c
+    is the chunk that holds the rows in the unswizzled line.  The tensor store
+    of a box of lines [i0, i0 + L) with i0 % 8 == 0, read through the line's
+    swizzle, must deliver element (u, i) of the destination block from where
+    row u's value of point i was written, for every (u, i), each staging byte
+    used once."""
+    ncw = 8 if es == 8 else 4
+    S = ncw * rpw
+    lb = S * es
+    assert lb in (64, 128)
+
+    def chunk(i, c):
+        return (c ^ (i & 7)) << 4 if lb == 128 else (c ^ ((i >> 1) & 3)) << 4
+
     written = {}
     for w in range(ncw):
-        ua = 2 * w
+        ua = rpw * w
         for i in range(M):
-            line = i * 128
-            if es == 8:
-                off = line + ((w ^ (i & 7)) << 4)
+            line = i * lb
+            if es == 8 and rpw == 2:
+                off = line + chunk(i, w)
                 written[off] = (ua, i)
                 written[off + 8] = (ua + 1, i)
+            elif es == 8:
+                written[line + chunk(i, ua >> 1) + 8 * (ua & 1)] = (ua, i)
             else:
-                written[line + ((ua ^ (i & 7)) << 4)] = (ua, i)
-                written[line + (((ua + 1) ^ (i & 7)) << 4)] = (ua + 1, i)
+                for r in range(rpw):
+                    written[line + chunk(i, ua + r)] = (ua + r, i)
     assert len(written) == S * M                         # every (row, point) once
-    for i0 in range(0, M, 128):
+    assert all(0 <= o and o + es <= M * lb for o in written)
+    for i0 in sorted({0, 8, 40} | set(range(0, M, 128))):
         L = min(256, M - i0)
         for i in range(i0, i0 + L):
             for u in range(S):
-                logical = (i - i0) * 128 + u * es         # box element (u, i): u fastest, 128-byte lines
-                phys = _tma_unswizzle_128b(i0 * 128 + logical)
+                logical = (i - i0) * lb + u * es          # box element (u, i): u fastest, lb-byte lines
+                phys = _tma_unswizzle(i0 * lb + logical, lb)
                 assert written[phys] == (u, i)
