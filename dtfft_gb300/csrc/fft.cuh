@@ -52,10 +52,13 @@ dtfft_error_t tc_execute(void* tc, const void* in, void* out, i64 nsig, int sign
 
 // Bluestein form of a batched transform whose length has a prime factor
 // above 127 (fft_bluestein.cu).  kind: 0 C2C, 1 real input (R2C, odd n),
-// 2 Hermitian half input (C2R, odd n).  Geometry as in the kernels' steps:
-// rows signal s at s*idist / s*odist, or columns (cols != 0) of planes.
+// 2 Hermitian half input (C2R, odd n), 3 R2R: the length-m core of mode
+// r2r_mode (M_DCT1 .. M_DST4) for r2r_n reals, with that mode's tables ta/tb.
+// Geometry as in the kernels' steps: rows signal s at s*idist / s*odist, or
+// columns (cols != 0) of planes.
 dtfft_error_t blue_create(int dbl, int m, int sign, int kind, i64 nsig, i64 idist, i64 odist, i64 plane, int ld,
-                          int ncols, int cols, void** out);
+                          int ncols, int cols, void** out, int r2r_mode = 0, int r2r_n = 0,
+                          const void* ta = nullptr, const void* tb = nullptr);
 dtfft_error_t blue_execute(void* b, const void* in, void* out, cudaStream_t s);
 void blue_destroy(void* b);
 

@@ -13,7 +13,11 @@
 // Rows go through in chunks so the L-point scratch stays bounded.  Real
 // input (R2C of odd length) and Hermitian input (C2R of odd length) are
 // expanded in chirp-in, and only the transform's own outputs are written in
-// chirp-out.
+// chirp-out.  An R2R kind (DCT/DST-I..IV) is a length-m complex FFT between
+// a pre- and a post-processing step; chirp-in builds the core sequence from
+// the signal's reals and chirp-out reads each output's core-spectrum point
+// (r2r_pre / r2r_post in fft_kernels.cuh, shared with the shared-memory
+// kernel).
 #include <cmath>
 #include <complex>
 #include <vector>
@@ -28,6 +32,9 @@ struct BlueGeom {
     i64 plane;          // columns: signal s = column s % ncols of plane s / ncols
     int ld, ncols;
     int cols;
+    int mode, n;        // R2R (kind 3): the core mode and the kind's length
+    const void* ta;     // R2R pre/post tables
+    const void* tb;
 };
 
 template <typename R>
@@ -36,7 +43,8 @@ __device__ __forceinline__ i64 blue_at(const BlueGeom& g, i64 s, int k, bool in)
     return s * (in ? g.idist : g.odist) + k;
 }
 
-// kind: 0 C2C, 1 real input (R2C, odd n), 2 Hermitian half input (C2R, odd n)
+// kind: 0 C2C, 1 real input (R2C, odd n), 2 Hermitian half input (C2R, odd n),
+// 3 R2R (the core sequence of mode g.mode)
 template <typename R>
 __global__ void blue_chirp_in(const void* in, typename CT<R>::T* a, const typename CT<R>::T* w, BlueGeom g,
                               i64 s0, int nrows, int m, int L, int kind) {
@@ -48,7 +56,11 @@ __global__ void blue_chirp_in(const void* in, typename CT<R>::T* a, const typena
         if (j < m) {
             const i64 s = s0 + r;
             C x;
-            if (kind == 1) {
+            if (kind == 3) {
+                const R* inR = reinterpret_cast<const R*>(in);
+                x = r2r_pre<R>(g.mode, g.n, m, j, [&](int i) { return inR[blue_at<R>(g, s, i, true)]; },
+                               reinterpret_cast<const C*>(g.ta));
+            } else if (kind == 1) {
                 x.x = reinterpret_cast<const R*>(in)[blue_at<R>(g, s, j, true)];
                 x.y = 0;
             } else if (kind == 2) {
@@ -75,12 +87,19 @@ template <typename R>
 __global__ void blue_chirp_out(const typename CT<R>::T* a, void* out, const typename CT<R>::T* w, BlueGeom g,
                                i64 s0, int nrows, int m, int L, int kind) {
     typedef typename CT<R>::T C;
-    const int nk = kind == 1 ? m / 2 + 1 : m;
+    const int nk = kind == 1 ? m / 2 + 1 : kind == 3 ? g.n : m;
     const i64 total = (i64)nrows * nk;
     for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
         const int r = (int)(e / nk), k = (int)(e - (i64)r * nk);
-        const C X = cmul(a[(i64)r * L + k], w[k]);
         const i64 o = blue_at<R>(g, s0 + r, k, false);
+        if (kind == 3) {
+            const int p = r2r_post_src(g.mode, g.n, k);
+            const C X = cmul(a[(i64)r * L + p], w[p]);
+            reinterpret_cast<R*>(out)[o] =
+                r2r_post<R>(g.mode, g.n, k, X, reinterpret_cast<const C*>(g.ta), reinterpret_cast<const C*>(g.tb));
+            continue;
+        }
+        const C X = cmul(a[(i64)r * L + k], w[k]);
         if (kind == 2) reinterpret_cast<R*>(out)[o] = X.x;
         else reinterpret_cast<C*>(out)[o] = X;
     }
@@ -133,12 +152,13 @@ static dtfft_error_t upload_c(const std::vector<std::complex<double>>& v, void**
 }
 
 dtfft_error_t blue_create(int dbl, int m, int sign, int kind, i64 nsig, i64 idist, i64 odist, i64 plane, int ld,
-                          int ncols, int cols, void** out) {
+                          int ncols, int cols, void** out, int r2r_mode, int r2r_n, const void* ta, const void* tb) {
     *out = nullptr;
-    if (m < 2 || nsig < 0) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    if (m < 2 || nsig < 0 || kind < 0 || kind > 3) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     Bluestein* b = new Bluestein();
     b->dbl = dbl; b->m = m; b->kind = kind; b->nsig = nsig;
     b->g.idist = idist; b->g.odist = odist; b->g.plane = plane; b->g.ld = ld; b->g.ncols = ncols; b->g.cols = cols;
+    b->g.mode = r2r_mode; b->g.n = r2r_n; b->g.ta = ta; b->g.tb = tb;
     int L = 1;
     while (L < 2 * m - 1) L <<= 1;
     b->L = L;

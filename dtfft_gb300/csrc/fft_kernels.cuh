@@ -249,6 +249,88 @@ __device__ __forceinline__ i64 gout(const Args<R>& A, i64 sig, int k) {
     return sig * A.odist + k;
 }
 
+// ---------------------------------------------------------------------------
+// R2R kinds as a length-m complex FFT (modes M_DCT1 .. M_DST4): point k of the
+// core sequence from the signal's n reals, and output k of the kind from one
+// point of the core spectrum.  Shared by the shared-memory kernel and the
+// Bluestein form (fft_bluestein.cu).
+// ---------------------------------------------------------------------------
+// x(j): real j of the signal; ta: W_4n^k (DCT/DST-II/-III/-IV)
+template <typename R, typename X>
+__device__ __forceinline__ typename CT<R>::T r2r_pre(int mode, int n, int m, int k, X x,
+                                                     const typename CT<R>::T* ta) {
+    typedef typename CT<R>::T C;
+    C v; v.x = 0; v.y = 0;
+    switch (mode) {
+    case M_DCT1:    // m = 2(n-1): even extension
+        v.x = x(k < n ? k : m - k);
+        break;
+    case M_DST1:    // m = 2(n+1): [0, x, 0, -rev x]
+        if (k >= 1 && k <= n) v.x = x(k - 1);
+        else if (k >= n + 2) v.x = -x(m - k - 1);
+        break;
+    case M_DCT2: case M_DST2: {   // m = n, Makhoul order: v[k] = x[2k] or x[2(n-1-k)+1]
+        const int j = (2 * k < n) ? 2 * k : 2 * (n - 1 - k) + 1;
+        R t = x(j);
+        if (mode == M_DST2 && (j & 1)) t = -t;
+        v.x = t;
+    } break;
+    case M_DCT3: case M_DST3: {   // m = n: V[k] = (X[k] - i X[n-k]) * conj(W_4n^k)
+        R a, b = 0;
+        if (mode == M_DCT3) {
+            a = x(k);
+            if (k > 0) b = x(n - k);
+        } else {                  // DST-III: X'[j] = x[n-1-j]
+            a = x(n - 1 - k);
+            if (k > 0) b = x(k - 1);
+        }
+        C t; t.x = a; t.y = -b;
+        v = cmul(t, cconj(ta[k]));
+    } break;
+    case M_DCT4: case M_DST4:     // m = 2n: x[j] * W_4n^j, zero padded
+        if (k < n) {
+            C t; t.x = x(mode == M_DCT4 ? k : n - 1 - k); t.y = 0;
+            v = cmul(t, ta[k]);
+        }
+        break;
+    }
+    return v;
+}
+
+// The core-spectrum point output k of the kind is made from.
+__device__ __forceinline__ int r2r_post_src(int mode, int n, int k) {
+    switch (mode) {
+    case M_DST1: return k + 1;
+    case M_DST2: return n - 1 - k;                                   // DST-II is DCT-II's order reversed
+    case M_DCT3: case M_DST3: return (k & 1) ? (n - 1 - (k >> 1)) : (k >> 1);
+    default: return k;
+    }
+}
+
+// Output k of the kind from f = core spectrum point r2r_post_src(mode, n, k);
+// tb: W_8n^(2k+1) (DCT/DST-IV).
+template <typename R>
+__device__ __forceinline__ R r2r_post(int mode, int n, int k, typename CT<R>::T f, const typename CT<R>::T* ta,
+                                      const typename CT<R>::T* tb) {
+    switch (mode) {
+    case M_DCT1: return f.x;
+    case M_DST1: return -f.y;
+    case M_DCT2: case M_DST2: {   // y = 2 Re(W_4n^p F[p])
+        const int p = mode == M_DCT2 ? k : n - 1 - k;
+        const typename CT<R>::T w = ta[p];
+        return (R)2 * (w.x * f.x - w.y * f.y);
+    }
+    case M_DCT3: return f.x;
+    case M_DST3: return (k & 1) ? -f.x : f.x;
+    case M_DCT4: case M_DST4: {
+        const typename CT<R>::T w = tb[k];
+        const R y = (R)2 * (w.x * f.x - w.y * f.y);
+        return (mode == M_DST4 && (k & 1)) ? -y : y;
+    }
+    }
+    return 0;
+}
+
 template <typename R, bool COLS>
 __global__ void __launch_bounds__(256) fft_kernel(Args<R> A) {
     typedef typename CT<R>::T C;
@@ -293,39 +375,9 @@ __global__ void __launch_bounds__(256) fft_kernel(Args<R> A) {
             if (k <= n / 2) { v = inC[gin<R, COLS>(A, sg, k)]; if (k == 0) v.y = 0; }
             else v = cconj(inC[gin<R, COLS>(A, sg, n - k)]);
         } break;
-        case M_DCT1: {  // m = 2(n-1): even extension
-            int j = k < n ? k : m - k;
-            v.x = inR[gin<R, COLS>(A, sg, j)];
-        } break;
-        case M_DST1: {  // m = 2(n+1): [0, x, 0, -rev x]
-            if (k >= 1 && k <= n) v.x = inR[gin<R, COLS>(A, sg, k - 1)];
-            else if (k >= n + 2) v.x = -inR[gin<R, COLS>(A, sg, m - k - 1)];
-        } break;
-        case M_DCT2: case M_DST2: {  // m = n, Makhoul order: v[k] = x[2k] or x[2(n-1-k)+1]
-            int j = (2 * k < n) ? 2 * k : 2 * (n - 1 - k) + 1;
-            R x = inR[gin<R, COLS>(A, sg, j)];
-            if (A.mode == M_DST2 && (j & 1)) x = -x;
-            v.x = x;
-        } break;
-        case M_DCT3: case M_DST3: {  // m = n: V[k] = (X[k] - i X[n-k]) * conj(W_4n^k)
-            R a, b = 0;
-            if (A.mode == M_DCT3) {
-                a = inR[gin<R, COLS>(A, sg, k)];
-                if (k > 0) b = inR[gin<R, COLS>(A, sg, n - k)];
-            } else {   // DST-III: X'[j] = x[n-1-j]
-                a = inR[gin<R, COLS>(A, sg, n - 1 - k)];
-                if (k > 0) b = inR[gin<R, COLS>(A, sg, k - 1)];
-            }
-            C t; t.x = a; t.y = -b;
-            v = cmul(t, cconj(A.ta[k]));
-        } break;
-        case M_DCT4: case M_DST4: {  // m = 2n: x[j] * W_4n^j, zero padded
-            if (k < n) {
-                R x = inR[gin<R, COLS>(A, sg, A.mode == M_DCT4 ? k : n - 1 - k)];
-                C t; t.x = x; t.y = 0;
-                v = cmul(t, A.ta[k]);
-            }
-        } break;
+        default:
+            v = r2r_pre<R>(A.mode, n, m, k, [&](int j) { return inR[gin<R, COLS>(A, sg, j)]; }, A.ta);
+            break;
         }
         bufA[sidx<COLS>(sl, k, pitch, per)] = v;
     }
@@ -364,29 +416,10 @@ __global__ void __launch_bounds__(256) fft_kernel(Args<R> A) {
             outR[gout<R, COLS>(A, sg, k)] = (k & 1) ? z.y : z.x;
         } break;
         case M_C2R_FULL: outR[gout<R, COLS>(A, sg, k)] = res[sidx<COLS>(sl, k, pitch, per)].x; break;
-        case M_DCT1: outR[gout<R, COLS>(A, sg, k)] = res[sidx<COLS>(sl, k, pitch, per)].x; break;
-        case M_DST1: outR[gout<R, COLS>(A, sg, k)] = -res[sidx<COLS>(sl, k + 1, pitch, per)].y; break;
-        case M_DCT2: case M_DST2: {
-            // y[k] = 2 Re(W_4n^k F[k]); DST-II writes it reversed
-            C f = res[sidx<COLS>(sl, k, pitch, per)];
-            C w = A.ta[k];
-            R y = (R)2 * (w.x * f.x - w.y * f.y);
-            outR[gout<R, COLS>(A, sg, A.mode == M_DCT2 ? k : n - 1 - k)] = y;
-        } break;
-        case M_DCT3: case M_DST3: {
-            // y[2j] = Re v[j], y[2j+1] = Re v[n-1-j]  (index k of the output)
-            int j = (k & 1) ? (n - 1 - (k >> 1)) : (k >> 1);
-            R y = res[sidx<COLS>(sl, j, pitch, per)].x;
-            if (A.mode == M_DST3 && (k & 1)) y = -y;
-            outR[gout<R, COLS>(A, sg, k)] = y;
-        } break;
-        case M_DCT4: case M_DST4: {
-            C f = res[sidx<COLS>(sl, k, pitch, per)];
-            C w = A.tb[k];
-            R y = (R)2 * (w.x * f.x - w.y * f.y);
-            if (A.mode == M_DST4 && (k & 1)) y = -y;
-            outR[gout<R, COLS>(A, sg, k)] = y;
-        } break;
+        default:
+            outR[gout<R, COLS>(A, sg, k)] =
+                r2r_post<R>(A.mode, n, k, res[sidx<COLS>(sl, r2r_post_src(A.mode, n, k), pitch, per)], A.ta, A.tb);
+            break;
         }
     }
 }
