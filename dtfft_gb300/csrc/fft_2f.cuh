@@ -1,0 +1,242 @@
+// Two-factor batched FFT for lengths m = M1 * M2 without a warp-aligned
+// schedule (odd 7-smooth lengths such as 105, 175, 225, 378): the four-step
+// decomposition inside one CTA, with both factor transforms held in one
+// thread's registers.  C2C rows and columns; rows of the real modes (R2C / C2R
+// through an m-point core: half length for even n, full length for odd n),
+// whose pre-processing is folded into phase A's loads and post-processing
+// into phase B's stores (R2C of even n pairs outputs k and m - k, so it
+// stages the core spectrum in shared memory for a phase C).
+//
+//   X[k1 + M1 k2] = sum_j2 W_M2^(j2 k2) [ W_m^(j2 k1) sum_j1 x[j2 + M2 j1] W_M1^(j1 k1) ]
+//
+// Phase A: for every (signal, j2) a thread loads the M1 points j2 + M2 j1
+// straight from global memory, transforms them (codelet DFT_M1), applies the
+// twiddles W_m^(j2 k1) and writes the row k1 of its signal's M1 x M2
+// intermediate into shared memory.  Phase B: for every (signal, k1) a thread
+// reads the M2 values of row k1, transforms them (DFT_M2) and stores outputs
+// k1 + M1 k2 straight to global memory.  One barrier per CTA; every point is
+// read from and written to HBM once.  Rows: consecutive threads take
+// consecutive j2 (k1) of a signal, the intermediate rows are padded to an odd
+// pitch so phase B's strided reads stay conflict-free.  Columns: consecutive
+// threads take consecutive signals (adjacent columns), so every load and
+// store is a contiguous run across the warp.
+//
+// The codelets are Cooley-Tukey in registers: DFT_N = DFT_P over the N/P
+// interleaved subsequences, twiddles W_N^(q k) as compile-time constants
+// (ktrig.h), then DFT_(N/P) recursively, with P the radix butterflies of
+// fft_kernels.cuh (2, 3, 4, 5, 7, 8, 16).
+#pragma once
+#include <type_traits>
+
+#include "fft_kernels.cuh"
+#include "ktrig.h"
+
+namespace gb {
+
+template <int B, int E, typename F>
+__device__ __forceinline__ void sfor(F&& f) {
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        sfor<B + 1, E>(f);
+    }
+}
+
+// Radix split of a codelet of N points: the first butterfly (16, 8, 7, 5, 4,
+// 3, 2) that divides N and leaves a second factor above 1.
+template <int N>
+constexpr int codelet_split() {
+    constexpr int cand[7] = {16, 8, 7, 5, 4, 3, 2};
+    for (int i = 0; i < 7; ++i)
+        if (N % cand[i] == 0 && N > cand[i]) return cand[i];
+    return N;
+}
+
+// v[k] <- sum_j v[j] exp(s 2 pi i j k / N), natural order in and out
+template <typename R, int N, typename C>
+__device__ __forceinline__ void dftc(C* v, int s) {
+    if constexpr (N == 1) {
+        (void)v; (void)s;
+    } else if constexpr (N == 2 || N == 3 || N == 4 || N == 5 || N == 7 || N == 8 || N == 16) {
+        dft_any<R, N>(v, s);
+    } else {
+        constexpr int P = codelet_split<N>(), Q = N / P;
+        static_assert(P * Q == N && Q > 1, "codelet split");
+        C a[Q][P];
+        sfor<0, Q>([&](auto qc) {
+            constexpr int q = decltype(qc)::value;
+            sfor<0, P>([&](auto rc) { a[q][decltype(rc)::value] = v[q + Q * decltype(rc)::value]; });
+            dft_any<R, P>(a[q], s);
+            if constexpr (q > 0) {
+                sfor<1, P>([&](auto kc) {
+                    constexpr int k = decltype(kc)::value;
+                    constexpr double c = ktrig::cos2pi((long long)q * k, N);
+                    constexpr double sn = ktrig::sin2pi((long long)q * k, N);
+                    C w;
+                    w.x = (R)c;
+                    w.y = s > 0 ? (R)sn : (R)-sn;
+                    a[q][k] = cmul(a[q][k], w);
+                });
+            }
+        });
+        sfor<0, P>([&](auto kc) {
+            constexpr int k1 = decltype(kc)::value;
+            C b[Q];
+            sfor<0, Q>([&](auto qc) { b[decltype(qc)::value] = a[decltype(qc)::value][k1]; });
+            dftc<R, Q>(b, s);
+            sfor<0, Q>([&](auto k2c) { v[k1 + P * decltype(k2c)::value] = b[decltype(k2c)::value]; });
+        });
+    }
+}
+
+template <typename R>
+struct F2Args {
+    typedef typename CT<R>::T C;
+    const void* in;
+    void* out;
+    const C* tw;            // W_m^e = exp(-2 pi i e / m), e < m
+    const C* ta;            // real modes: the pre/post twiddles of the shared-memory kernel's modes
+    int n;                  // real modes: reals per signal
+    i64 nsig;
+    i64 idist, odist;       // rows: signal s at s * idist / s * odist, unit stride
+    i64 plane;              // columns: signal s = column s % ncols of plane s / ncols,
+    int ld, ncols;          //          point k at k * ld
+    int sign;
+    int per;                // signals per CTA
+};
+
+template <typename R, bool COLS>
+__device__ __forceinline__ i64 f2_at(const F2Args<R>& A, i64 s, int k, bool in) {
+    if (COLS) return (s / A.ncols) * A.plane + (s % A.ncols) + (i64)k * A.ld;
+    return s * (in ? A.idist : A.odist) + k;
+}
+
+// Point j of the core sequence of signal sg (phase A).
+template <typename R, int MODE, bool COLS>
+__device__ __forceinline__ typename CT<R>::T f2_load(const F2Args<R>& A, i64 sg, int j, int m) {
+    typedef typename CT<R>::T C;
+    const C* inC = reinterpret_cast<const C*>(A.in);
+    const R* inR = reinterpret_cast<const R*>(A.in);
+    C v;
+    if constexpr (MODE == M_C2C) {
+        v = inC[f2_at<R, COLS>(A, sg, j, true)];
+    } else if constexpr (MODE == M_R2C_HALF) {      // z[j] = x[2j] + i x[2j+1]
+        const i64 g = f2_at<R, COLS>(A, sg, 2 * j, true);
+        v.x = inR[g]; v.y = inR[g + 1];
+    } else if constexpr (MODE == M_R2C_FULL) {
+        v.x = inR[f2_at<R, COLS>(A, sg, j, true)]; v.y = 0;
+    } else if constexpr (MODE == M_C2R_HALF) {      // Z[j] = E[j] + i O[j] from X[j], X[m - j]
+        C xk = inC[f2_at<R, COLS>(A, sg, j, true)];
+        C xm = inC[f2_at<R, COLS>(A, sg, m - j, true)];
+        if (j == 0) { xk.y = 0; xm.y = 0; }
+        const C cxm = cconj(xm);
+        const C e = cadd(xk, cxm);
+        const C o = cmul(csub(xk, cxm), cconj(A.ta[j]));
+        v = cadd(e, cmul_is(o, 1));
+    } else {                                        // M_C2R_FULL: Hermitian extension
+        if (j <= A.n / 2) { v = inC[f2_at<R, COLS>(A, sg, j, true)]; if (j == 0) v.y = 0; }
+        else v = cconj(inC[f2_at<R, COLS>(A, sg, A.n - j, true)]);
+    }
+    return v;
+}
+
+// Core spectrum point k of signal sg (phase B); R2C of even n keeps it in zs.
+template <typename R, int MODE, bool COLS>
+__device__ __forceinline__ void f2_store(const F2Args<R>& A, i64 sg, int k, typename CT<R>::T z,
+                                         typename CT<R>::T* zs) {
+    typedef typename CT<R>::T C;
+    C* outC = reinterpret_cast<C*>(A.out);
+    R* outR = reinterpret_cast<R*>(A.out);
+    if constexpr (MODE == M_C2C) {
+        outC[f2_at<R, COLS>(A, sg, k, false)] = z;
+    } else if constexpr (MODE == M_R2C_HALF) {
+        zs[k] = z;
+    } else if constexpr (MODE == M_R2C_FULL) {
+        if (k <= A.n / 2) outC[f2_at<R, COLS>(A, sg, k, false)] = z;
+    } else if constexpr (MODE == M_C2R_HALF) {      // y[2k] = Re z, y[2k+1] = Im z
+        const i64 g = f2_at<R, COLS>(A, sg, 2 * k, false);
+        outR[g] = z.x; outR[g + 1] = z.y;
+    } else {
+        outR[f2_at<R, COLS>(A, sg, k, false)] = z.x;
+    }
+}
+
+template <typename R, int M1, int M2, int MODE, bool COLS>
+__global__ void __launch_bounds__(256) fft2f_kernel(const F2Args<R> A) {
+    typedef typename CT<R>::T C;
+    constexpr int M = M1 * M2;
+    constexpr int PR = M2 | 1;   // rows: odd pitch of an intermediate row
+    static_assert(MODE == M_C2C || !COLS, "real modes run along rows");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* ys = reinterpret_cast<C*>(smem_raw);
+    const int per = A.per;
+    C* zs = ys + (size_t)per * M1 * PR;            // R2C of even n: the core spectra
+    const i64 s0 = (i64)blockIdx.x * per;
+    const int ns = (int)min((i64)per, A.nsig - s0);
+    if (ns <= 0) return;
+    const int s = A.sign;
+    // intermediate (signal sl, row k1, column j2)
+    auto yat = [&](int sl, int k1, int j2) -> int {
+        return COLS ? (k1 * M2 + j2) * per + sl : (sl * M1 + k1) * PR + j2;
+    };
+
+    for (int it = threadIdx.x; it < ns * M2; it += blockDim.x) {
+        int sl, j2;
+        if (COLS) { j2 = it / ns; sl = it - j2 * ns; } else { sl = it / M2; j2 = it - sl * M2; }
+        const i64 sg = s0 + sl;
+        C v[M1];
+#pragma unroll
+        for (int j1 = 0; j1 < M1; ++j1) v[j1] = f2_load<R, MODE, COLS>(A, sg, j2 + M2 * j1, M);
+        dftc<R, M1>(v, s);
+        int e = 0;   // j2 * k1 mod M
+#pragma unroll
+        for (int k1 = 1; k1 < M1; ++k1) {
+            e += j2;
+            if (e >= M) e -= M;
+            C w = __ldg(&A.tw[e]);
+            if (s > 0) w.y = -w.y;
+            v[k1] = cmul(v[k1], w);
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < M1; ++k1) ys[yat(sl, k1, j2)] = v[k1];
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < ns * M1; it += blockDim.x) {
+        int sl, k1;
+        if (COLS) { k1 = it / ns; sl = it - k1 * ns; } else { sl = it / M1; k1 = it - sl * M1; }
+        const i64 sg = s0 + sl;
+        C u[M2];
+#pragma unroll
+        for (int j2 = 0; j2 < M2; ++j2) u[j2] = ys[yat(sl, k1, j2)];
+        dftc<R, M2>(u, s);
+#pragma unroll
+        for (int k2 = 0; k2 < M2; ++k2) f2_store<R, MODE, COLS>(A, sg, k1 + M1 * k2, u[k2], zs + (size_t)sl * M);
+    }
+    if constexpr (MODE == M_R2C_HALF) {
+        // phase C: X[k] = E[k] - i W_n^k O[k], E / O from Z[k] and conj Z[m - k], k <= m
+        __syncthreads();
+        C* outC = reinterpret_cast<C*>(A.out);
+        for (int it = threadIdx.x; it < ns * (M + 1); it += blockDim.x) {
+            const int sl = it / (M + 1), k = it - sl * (M + 1);
+            const C* z = zs + (size_t)sl * M;
+            const C zk = z[k == M ? 0 : k];
+            const C zm = cconj(z[k == 0 ? 0 : M - k]);
+            const C e = cscale(cadd(zk, zm), (R)0.5);
+            const C o = cscale(csub(zk, zm), (R)0.5);
+            const C t = cmul(A.ta[k], o);
+            outC[f2_at<R, COLS>(A, s0 + sl, k, false)] = cadd(e, cmul_is(t, -1));
+        }
+    }
+}
+
+// Shared memory of a CTA of `per` signals.
+inline size_t f2_smem(int m1, int m2, bool cols, int per, size_t es, int mode) {
+    if (cols) return (size_t)m1 * m2 * per * es;
+    return (size_t)per * m1 * (m2 | 1) * es + (mode == M_R2C_HALF ? (size_t)per * m1 * m2 * es : 0);
+}
+
+// Compiled two-factor kernels (fft_2f_f32_*.cu): the kernel for a core of m
+// points (float) in `mode` (C2C rows or columns; R2C / C2R rows), its
+// factors; nullptr when none is compiled.
+void* f2_kernel_f32(int m, bool cols, int mode, int* m1, int* m2);
+
+}  // namespace gb

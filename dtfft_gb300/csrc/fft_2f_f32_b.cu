@@ -1,0 +1,39 @@
+// Two-factor FFT kernels (fft_2f.cuh), float C2C rows and columns, lengths
+// 105..196: the most balanced split m = M1 * M2 with both factors at most 49.
+#include "fft_2f.cuh"
+
+namespace gb {
+
+void* f2_kernel_f32_b(int m, bool cols, int mode, int* m1, int* m2) {
+    if (mode != M_C2C) return nullptr;
+#define GB_F2(M_, A_, B_)                                                                        \
+    case M_:                                                                                    \
+        *m1 = A_; *m2 = B_;                                                                     \
+        return cols ? (void*)fft2f_kernel<float, A_, B_, M_C2C, true>                         \
+                    : (void*)fft2f_kernel<float, A_, B_, M_C2C, false>;
+    switch (m) {
+    GB_F2(105, 7, 15)
+    GB_F2(108, 9, 12)
+    GB_F2(112, 8, 14)
+    GB_F2(120, 10, 12)
+    GB_F2(125, 5, 25)
+    GB_F2(126, 9, 14)
+    GB_F2(135, 9, 15)
+    GB_F2(140, 10, 14)
+    GB_F2(144, 12, 12)
+    GB_F2(147, 7, 21)
+    GB_F2(150, 10, 15)
+    GB_F2(160, 10, 16)
+    GB_F2(162, 9, 18)
+    GB_F2(168, 12, 14)
+    GB_F2(175, 7, 25)
+    GB_F2(180, 12, 15)
+    GB_F2(189, 9, 21)
+    GB_F2(192, 12, 16)
+    GB_F2(196, 14, 14)
+    }
+#undef GB_F2
+    return nullptr;
+}
+
+}  // namespace gb

@@ -9,6 +9,7 @@
 #include <mutex>
 #include <sstream>
 
+#include "fft_2f.cuh"
 #include "fft_kernels.cuh"
 #include "fft_tile.cuh"
 
@@ -128,6 +129,9 @@ struct FftStep {
     int tile_S = 0, tile_nst = 0, tile_threads = 0, tile_nw = 0;
     size_t tile_smem = 0;
     const void* tw_dir = nullptr;   // W_m^(sign*e) for this step's direction
+    void* f2 = nullptr;      // C2C float: two-factor kernel (fft_2f.cuh), f2_m1 x f2_m2, f2_per signals per CTA
+    int f2_m1 = 0, f2_m2 = 0, f2_per = 0;
+    size_t f2_smem = 0;
     ~FftStep() { tc_destroy(tc); blue_destroy(blue); }
 };
 
@@ -356,6 +360,7 @@ static dtfft_error_t prepare_launch(const FftStep& S) {
 }
 
 static dtfft_error_t upload_mode_tables(FftStep& S, std::vector<void*>& owned);
+static void f2_prefer(FftStep& S, std::vector<void*>& owned);
 
 static dtfft_error_t prepare_step(FftStep& S, std::vector<void*>& owned) {
     // DCT/DST-II and -III of even length through an n/2-point complex FFT when
@@ -519,6 +524,26 @@ static dtfft_error_t launch_pipe(const PArgs<R>& P, int E, int threads, size_t s
 template <typename R, bool COLS>
 static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, cudaStream_t s) {
     if (S.blue) return blue_execute(S.blue, in, out, s);
+    if (S.f2) {
+        F2Args<R> F;
+        F.in = in; F.out = out; F.tw = (const typename CT<R>::T*)S.tw; F.ta = (const typename CT<R>::T*)S.ta;
+        F.n = S.n; F.nsig = S.nsig; F.idist = S.idist; F.odist = S.odist; F.plane = S.plane; F.ld = S.ld; F.ncols = S.ncols;
+        F.sign = S.sign; F.per = S.f2_per;
+        const i64 ctas = (S.nsig + S.f2_per - 1) / S.f2_per;
+        if (ctas <= 0) return DTFFT_SUCCESS;
+        if (ctas > 0x7fffffffLL) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+        void (*kfn)(F2Args<R>) = (void (*)(F2Args<R>))S.f2;
+        void* tok = prof_begin(s);
+        kfn<<<(unsigned)ctas, 256, S.f2_smem, s>>>(F);
+        if (tok) {
+            static const char* mn[] = {"c2c", "r2c", "r2c", "c2r", "c2r"};
+            prof_end(tok, std::string("fft2f_") + (COLS ? "cols_" : "rows_") + mn[S.mode] + "_m" + std::to_string(S.m) +
+                              "_f32", s);
+        }
+        count_launch();
+        GB_CUDA_TRY(cudaGetLastError());
+        return DTFFT_SUCCESS;
+    }
     if (S.tc) {
         void* tok = prof_begin(s);
         GB_TRY(tc_execute(S.tc, in, out, S.nsig, S.sign, status_ptr(), s));
@@ -659,6 +684,7 @@ dtfft_error_t FftPlan::build(int sign, std::vector<FftStep*>& steps) {
     row->idist = in_row; row->odist = out_row;
     dtfft_error_t e = prepare_step(*row, tables_);
     if (e != DTFFT_SUCCESS) { delete row; return e; }
+    f2_prefer(*row, tables_);
 
     FftStep* col = nullptr;
     if (d.rank == 2) {
@@ -676,6 +702,7 @@ dtfft_error_t FftPlan::build(int sign, std::vector<FftStep*>& steps) {
         }
         e = prepare_step(*col, tables_);
         if (e != DTFFT_SUCCESS) { delete row; delete col; return e; }
+        f2_prefer(*col, tables_);
     }
     if (d.rank == 2 && d.type == FFT_R2C && sign == FFT_BWD) {
         col->reads_out = false;
@@ -717,7 +744,7 @@ dtfft_error_t FftPlan::execute(const void* in, void* out, int sign, cudaStream_t
 // fastest is kept.  Choices are cached per (GPU, library version, step
 // geometry) in the process and, with DTFFT_GB_TUNE_CACHE, in that file.
 struct StepCand {
-    enum Kind { TILE, PIPE, REG, SMEM } kind = SMEM;
+    enum Kind { TILE, PIPE, REG, SMEM, F2 } kind = SMEM;
     int E = 0, per = 1, S = 0, nst = 0;
     std::vector<int> radix;
     std::string name() const {
@@ -725,6 +752,7 @@ struct StepCand {
         switch (kind) {
         case TILE: o << "tile:S" << S << ":nst" << nst; break;
         case SMEM: o << "smem"; break;
+        case F2: o << "f2:per" << per; break;
         default: {
             o << (kind == PIPE ? "pipe:E" : "reg:E") << E << ":";
             for (size_t i = 0; i < radix.size(); ++i) o << (i ? "x" : "") << radix[i];
@@ -736,6 +764,10 @@ struct StepCand {
     static bool parse(const std::string& t, StepCand& c) {
         c = StepCand();
         if (t == "smem") { c.kind = SMEM; return true; }
+        if (t.compare(0, 3, "f2:") == 0) {
+            c.kind = F2;
+            return sscanf(t.c_str(), "f2:per%d", &c.per) == 1 && c.per > 0;
+        }
         if (t.compare(0, 5, "tile:") == 0) {
             c.kind = TILE;
             return sscanf(t.c_str(), "tile:S%d:nst%d", &c.S, &c.nst) == 2;
@@ -784,7 +816,17 @@ static bool apply_cand(FftStep& S, const StepCand& c, std::vector<void*>& owned)
     const bool c2c_rows = !S.cols && S.mode == M_C2C && S.idist == m && S.odist == m;
     S.tile = false;
     S.pipe = false;
+    S.f2 = nullptr;
     switch (c.kind) {
+    case StepCand::F2: {
+        int a = 0, b = 0;
+        void* fn = (S.dbl || S.mode > M_C2R_FULL) ? nullptr : f2_kernel_f32(m, S.cols, S.mode, &a, &b);
+        if (!fn || c.per < 1) return false;
+        const size_t smem = f2_smem(a, b, S.cols, c.per, es, S.mode);
+        if (smem > max_optin_smem() || set_smem_attrs(fn, smem) != DTFFT_SUCCESS) { cudaGetLastError(); return false; }
+        S.f2 = fn; S.f2_m1 = a; S.f2_m2 = b; S.f2_per = c.per; S.f2_smem = smem;
+        return true;
+    }
     case StepCand::TILE: {
         if (!c2c_rows) return false;
         const void* fn = S.dbl ? TilePtr<double>::get(m, S.sign, false) : TilePtr<float>::get(m, S.sign, false);
@@ -858,6 +900,25 @@ static bool apply_cand(FftStep& S, const StepCand& c, std::vector<void*>& owned)
     return false;
 }
 
+// C2C, R2C and C2R float steps without a tile kernel take the two-factor
+// kernel when one is compiled for their core length (measured faster than the register, pipelined
+// and shared-memory kernels on most such lengths; EXHAUSTIVE plans time them
+// all).  DTFFT_GB_F2=0: never; DTFFT_GB_F2=1: also over the tile kernels.
+static void f2_prefer(FftStep& S, std::vector<void*>& owned) {
+    const char* e = getenv("DTFFT_GB_F2");
+    const bool never = e && strcmp(e, "0") == 0, always = e && strcmp(e, "1") == 0;
+    if (never || S.tc || S.blue || S.dbl || S.mode > M_C2R_FULL || (S.tile && !always)) return;
+    int a = 0, b = 0;
+    if (!f2_kernel_f32(S.m, S.cols, S.mode, &a, &b)) return;
+    StepCand c;
+    c.kind = StepCand::F2;
+    c.per = S.cols ? 32 : (256 + std::min(a, b) - 1) / std::min(a, b);
+    FftStep t = S;
+    t.tc = nullptr; t.blue = nullptr;
+    if (apply_cand(t, c, owned)) S = t;
+    t.tc = nullptr; t.blue = nullptr;
+}
+
 static std::vector<StepCand> step_candidates(const FftStep& S) {
     std::vector<StepCand> out;
     const int m = S.m;
@@ -906,6 +967,20 @@ static std::vector<StepCand> step_candidates(const FftStep& S) {
     }
     Schedule sc;
     if (make_schedule(m, sc) && !half_mode(S.mode)) out.push_back(StepCand());   // smem
+    int a = 0, b = 0;
+    if (!S.dbl && S.mode <= M_C2R_FULL && f2_kernel_f32(m, S.cols, S.mode, &a, &b)) {
+        // rows: enough signals for 256 threads in the phase of the smaller factor, half and twice
+        // that; columns: runs of 16, 32 or 64 adjacent columns
+        const int base = (256 + std::min(a, b) - 1) / std::min(a, b);
+        const std::vector<int> pers =
+            S.cols ? std::vector<int>{16, 32, 64} : std::vector<int>{std::max(1, base / 2), base, 2 * base};
+        for (int per : pers) {
+            if (f2_smem(a, b, S.cols, per, es, S.mode) > 100 * 1024) continue;
+            StepCand c;
+            c.kind = StepCand::F2; c.per = per;
+            out.push_back(c);
+        }
+    }
     return out;
 }
 

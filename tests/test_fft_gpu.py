@@ -202,6 +202,100 @@ def test_tensor_store_fused_pass(dt, orc, cuda, monkeypatch, dims, grid):
     plan.destroy()
 
 
+@pytest.mark.parametrize("n,howmany", [(105, 777), (378, 300), (225, 1001), (343, 100), (40, 5000), (400, 64),
+                                        (245, 3)])
+def test_two_factor_rows(dt, cuda, monkeypatch, n, howmany):
+    """Batched C2C rows on the two-factor kernel (fft_2f.cuh; DTFFT_GB_F2=1
+    makes every C2C float step with a compiled split take it): forward and
+    backward against numpy FP64, ragged last CTA included."""
+    import torch
+    monkeypatch.setenv("DTFFT_GB_F2", "1")
+    L = dt.lib()
+    h = ctypes.c_void_p()
+    sizes = (ctypes.c_int32 * 1)(n)
+    assert L.gb_fft_create(1, 0, 0, n, n, howmany, sizes, sizes, sizes, None, None, ctypes.byref(h)) == 0
+    rng = np.random.default_rng(n)
+    x = (rng.uniform(-1, 1, (howmany, n)) + 1j * rng.uniform(-1, 1, (howmany, n))).astype(np.complex64)
+    a = torch.from_numpy(x).to(cuda)
+    b = torch.empty_like(a)
+    torch.cuda.synchronize()
+    L.dtfft_gb_profile_start()
+    assert L.gb_fft_execute(h, a.data_ptr(), b.data_ptr(), -1) == 0
+    torch.cuda.synchronize()
+    fwd = b.cpu().numpy()
+    assert L.gb_fft_execute(h, b.data_ptr(), a.data_ptr(), 1) == 0
+    torch.cuda.synchronize()
+    L.dtfft_gb_profile_stop()
+    assert ("fft2f_rows_c2c_m%d_f32" % n) in _profiled_names(L)
+    ref = np.fft.fft(x.astype(np.complex128), axis=1)
+    assert np.linalg.norm(fwd - ref) / np.linalg.norm(ref) <= 1e-5
+    back = a.cpu().numpy() / n
+    assert np.linalg.norm(back - x) / np.linalg.norm(x) <= 1e-5
+    assert L.gb_fft_destroy(ctypes.byref(h)) == 0
+
+
+@pytest.mark.parametrize("n,howmany", [(350, 513), (245, 77), (96, 1000), (756, 31), (125, 300), (80, 7)])
+def test_two_factor_real_rows(dt, cuda, monkeypatch, n, howmany):
+    """R2C / C2R rows on the two-factor kernel: even n through the n/2-point
+    core (R2C pairs outputs k and n/2 - k in a third phase), odd n through the
+    full-length core; against numpy FP64."""
+    import torch
+    monkeypatch.setenv("DTFFT_GB_F2", "1")
+    L = dt.lib()
+    h = ctypes.c_void_p()
+    sizes = (ctypes.c_int32 * 1)(n)
+    nc = n // 2 + 1
+    assert L.gb_fft_create(1, 1, 0, n, nc, howmany, sizes, sizes, sizes, None, None, ctypes.byref(h)) == 0
+    x = np.random.default_rng(n).standard_normal((howmany, n)).astype(np.float32)
+    a = torch.from_numpy(x).to(cuda)
+    b = torch.empty((howmany, nc), dtype=torch.complex64, device=cuda)
+    torch.cuda.synchronize()
+    L.dtfft_gb_profile_start()
+    assert L.gb_fft_execute(h, a.data_ptr(), b.data_ptr(), -1) == 0
+    torch.cuda.synchronize()
+    fwd = b.cpu().numpy()
+    c = torch.empty_like(a)
+    assert L.gb_fft_execute(h, b.data_ptr(), c.data_ptr(), 1) == 0
+    torch.cuda.synchronize()
+    L.dtfft_gb_profile_stop()
+    names = _profiled_names(L)
+    assert ("fft2f_rows_r2c_m%d_f32" % (n // 2 if n % 2 == 0 else n)) in names, names
+    assert ("fft2f_rows_c2r_m%d_f32" % (n // 2 if n % 2 == 0 else n)) in names, names
+    ref = np.fft.rfft(x.astype(np.float64), axis=1)
+    assert np.linalg.norm(fwd - ref) / np.linalg.norm(ref) <= 1e-5
+    back = c.cpu().numpy() / n
+    assert np.linalg.norm(back - x) / np.linalg.norm(x) <= 1e-5
+    assert L.gb_fft_destroy(ctypes.byref(h)) == 0
+
+
+@pytest.mark.parametrize("kind,dims", [("c2c", [64, 105, 40]), ("c2c", [75, 378, 49]), ("r2c", [48, 175, 56]),
+                                       ("c2c", [50, 343, 40])])
+def test_two_factor_columns_in_z_slab_plans(dt, orc, cuda, monkeypatch, kind, dims):
+    """Z-slab plans whose Y columns (and X / Z rows) take the two-factor kernel."""
+    monkeypatch.setenv("DTFFT_GB_F2", "1")
+    L = dt.lib()
+    np_dtype = np.complex64 if kind == "c2c" else np.float32
+    mk = dt.PlanC2C if kind == "c2c" else dt.PlanR2C
+    plan = mk(dims, precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT)
+    assert plan.z_slab_enabled
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=43)
+    x = orc.global_to_packed(g, 3, [1, 1, 1], 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, np.complex64, cuda)
+    expect = orc.global_to_packed(orc.forward_values(g, kind), 3, [1, 1, 1], _final_layout(plan, 3))
+    L.dtfft_gb_profile_start()
+    plan.execute(a, b, dt.Execute.FORWARD)
+    fwd = from_dev(b, expect.size, np.complex64)
+    c = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    L.dtfft_gb_profile_stop()
+    assert ("fft2f_cols_c2c_m%d_f32" % dims[1]) in _profiled_names(L)
+    assert orc.rel_l2(fwd, expect) <= 1e-5
+    back = from_dev(c, x.size, np_dtype).astype(np.complex128) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= 1e-5
+    plan.destroy()
+
+
 @pytest.mark.parametrize("dims,grid,np_dtype", [
     ([512, 64, 32], [1, 2, 2], np.complex64),
     ([256, 48, 256], [1, 1, 2], np.complex128),
