@@ -130,7 +130,7 @@ struct FftStep {
     size_t tile_smem = 0;
     const void* tw_dir = nullptr;   // W_m^(sign*e) for this step's direction
     void* f2 = nullptr;      // C2C float: two-factor kernel (fft_2f.cuh), f2_m1 x f2_m2, f2_per signals per CTA
-    int f2_m1 = 0, f2_m2 = 0, f2_per = 0;
+    int f2_m1 = 0, f2_m2 = 0, f2_per = 0, f2_threads = 256;
     size_t f2_smem = 0;
     ~FftStep() { tc_destroy(tc); blue_destroy(blue); }
 };
@@ -534,7 +534,7 @@ static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, 
         if (ctas > 0x7fffffffLL) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
         void (*kfn)(F2Args<R>) = (void (*)(F2Args<R>))S.f2;
         void* tok = prof_begin(s);
-        kfn<<<(unsigned)ctas, 256, S.f2_smem, s>>>(F);
+        kfn<<<(unsigned)ctas, S.f2_threads, S.f2_smem, s>>>(F);
         if (tok) {
             static const char* mn[] = {"c2c", "r2c", "r2c", "c2r", "c2r"};
             prof_end(tok, std::string("fft2f_") + (COLS ? "cols_" : "rows_") + mn[S.mode] + "_m" + std::to_string(S.m) +
@@ -752,7 +752,7 @@ struct StepCand {
         switch (kind) {
         case TILE: o << "tile:S" << S << ":nst" << nst; break;
         case SMEM: o << "smem"; break;
-        case F2: o << "f2:per" << per; break;
+        case F2: o << "f2:t" << S << ":per" << per; break;
         default: {
             o << (kind == PIPE ? "pipe:E" : "reg:E") << E << ":";
             for (size_t i = 0; i < radix.size(); ++i) o << (i ? "x" : "") << radix[i];
@@ -766,7 +766,8 @@ struct StepCand {
         if (t == "smem") { c.kind = SMEM; return true; }
         if (t.compare(0, 3, "f2:") == 0) {
             c.kind = F2;
-            return sscanf(t.c_str(), "f2:per%d", &c.per) == 1 && c.per > 0;
+            return sscanf(t.c_str(), "f2:t%d:per%d", &c.S, &c.per) == 2 && c.per > 0 &&
+                   (c.S == 32 || c.S == 64 || c.S == 128 || c.S == 256);
         }
         if (t.compare(0, 5, "tile:") == 0) {
             c.kind = TILE;
@@ -825,6 +826,7 @@ static bool apply_cand(FftStep& S, const StepCand& c, std::vector<void*>& owned)
         const size_t smem = f2_smem(a, b, S.cols, c.per, es, S.mode);
         if (smem > max_optin_smem() || set_smem_attrs(fn, smem) != DTFFT_SUCCESS) { cudaGetLastError(); return false; }
         S.f2 = fn; S.f2_m1 = a; S.f2_m2 = b; S.f2_per = c.per; S.f2_smem = smem;
+        S.f2_threads = (c.S == 32 || c.S == 64 || c.S == 128) ? c.S : 256;
         return true;
     }
     case StepCand::TILE: {
@@ -912,7 +914,15 @@ static void f2_prefer(FftStep& S, std::vector<void*>& owned) {
     if (!f2_kernel_f32(S.m, S.cols, S.mode, &a, &b)) return;
     StepCand c;
     c.kind = StepCand::F2;
-    c.per = S.cols ? 32 : (256 + std::min(a, b) - 1) / std::min(a, b);
+    // 128-thread CTAs of few signals (half of what fills the threads in the phase of the smaller
+    // factor) measured fastest on rows: more CTAs per SM overlap their load and transform phases
+    c.S = 128;
+    if (const char* v = getenv("DTFFT_GB_F2_THREADS")) {   // measurements
+        const int t = atoi(v);
+        c.S = (t == 32 || t == 64 || t == 256) ? t : 128;
+    }
+    c.per = S.cols ? 32 : std::max(1, (c.S + std::min(a, b) - 1) / std::min(a, b) / 2);
+    if (const char* v = getenv("DTFFT_GB_F2_PER")) c.per = std::max(1, atoi(v));
     FftStep t = S;
     t.tc = nullptr; t.blue = nullptr;
     if (apply_cand(t, c, owned)) S = t;
@@ -969,16 +979,21 @@ static std::vector<StepCand> step_candidates(const FftStep& S) {
     if (make_schedule(m, sc) && !half_mode(S.mode)) out.push_back(StepCand());   // smem
     int a = 0, b = 0;
     if (!S.dbl && S.mode <= M_C2R_FULL && f2_kernel_f32(m, S.cols, S.mode, &a, &b)) {
-        // rows: enough signals for 256 threads in the phase of the smaller factor, half and twice
-        // that; columns: runs of 16, 32 or 64 adjacent columns
-        const int base = (256 + std::min(a, b) - 1) / std::min(a, b);
-        const std::vector<int> pers =
-            S.cols ? std::vector<int>{16, 32, 64} : std::vector<int>{std::max(1, base / 2), base, 2 * base};
-        for (int per : pers) {
-            if (f2_smem(a, b, S.cols, per, es, S.mode) > 100 * 1024) continue;
-            StepCand c;
-            c.kind = StepCand::F2; c.per = per;
-            out.push_back(c);
+        // CTAs of 64, 128 or 256 threads; rows: a quarter, half and all of the signals that
+        // fill the threads in the phase of the smaller factor; columns: runs of 16, 32 or 64
+        // adjacent columns
+        for (int nt : {64, 128, 256}) {
+            const int base = (nt + std::min(a, b) - 1) / std::min(a, b);
+            const std::vector<int> pers = S.cols ? std::vector<int>{16, 32, 64}
+                                                 : std::vector<int>{std::max(1, base / 4), std::max(1, base / 2), base};
+            for (int per : pers) {
+                if (f2_smem(a, b, S.cols, per, es, S.mode) > 100 * 1024) continue;
+                StepCand c;
+                c.kind = StepCand::F2; c.per = per; c.S = nt;
+                bool dup = false;
+                for (const StepCand& o : out) dup = dup || (o.kind == c.kind && o.per == c.per && o.S == c.S);
+                if (!dup) out.push_back(c);
+            }
         }
     }
     return out;
