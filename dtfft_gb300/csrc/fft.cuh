@@ -89,7 +89,8 @@ class FusedFT {
 public:
     // Fails (without side effects) when the boxes do not give every source
     // rank whole rows of the transform axis or the length has no register
-    // schedule; with tile_only, also when the tile kernel cannot take the rows.
+    // schedule; with tile_only, also when neither the tile kernel nor the
+    // two-factor kernel (float) can take the rows.
     static dtfft_error_t create(const BoxList& bl, int m, int dbl, bool tile_only, FusedFT** out);
     ~FusedFT();
     dtfft_error_t execute(const void* in, void* out, int sign, cudaStream_t s);
@@ -118,6 +119,9 @@ private:
     // null when the pass's segments do not fit it or `use_xtma_` is off
     struct XTma* xtma_ = nullptr;
     bool use_xtma_ = false;
+    // two-factor kernel fused with the transpose (fft_2f.cuh), tiles of S_ rows
+    void* f2_ = nullptr;
+    int f2_threads_ = 128;
     Schedule sched_;
     const void* tw_ = nullptr;
     const void* groups_ = nullptr;

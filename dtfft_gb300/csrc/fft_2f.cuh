@@ -228,6 +228,98 @@ __global__ void __launch_bounds__(256) fft2f_kernel(const F2Args<R> A) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Fused with the box-list transpose: a CTA takes a tile of S rows (u0 .. u0+S-1
+// at one w) of one source rank's block (FGroup, as the tile kernels), runs
+// phase A on them as above and, in phase B, writes output point i of row u to
+// its destination rank's block (the FSeg holding i): dst_off + (i - i0) di +
+// u + w dw.  The intermediate is kept row-fastest ((k1 M2 + j2) * P + r, P = S
+// odd-padded) so that phase B's consecutive threads take consecutive rows and
+// store runs of S adjacent destination points.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct F2XArgs {
+    typedef typename CT<R>::T C;
+    const C* in;
+    C* out;
+    const C* tw;
+    const FGroup* groups;
+    const FSeg* segs;
+    int ngroups;
+    int S;                  // rows per tile
+    int sign;
+};
+
+template <typename R, int M1, int M2>
+__global__ void __launch_bounds__(256) fft2f_xpose_kernel(const F2XArgs<R> A) {
+    typedef typename CT<R>::T C;
+    constexpr int M = M1 * M2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* ys = reinterpret_cast<C*>(smem_raw);
+    const int S = A.S, P = A.S | 1;
+    const i64 tile = blockIdx.x;
+    int lo = 0, hi = A.ngroups - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.groups[mid].cta_begin <= tile) lo = mid; else hi = mid - 1;
+    }
+    const FGroup& g = A.groups[lo];
+    const int tl = (int)(tile - g.cta_begin);
+    const int u0 = (tl % g.tiles_u) * S, w = tl / g.tiles_u;
+    const int nrows = min(S, g.nu - u0);
+    const i64 row0 = g.src_off + (i64)u0 * g.su + (i64)w * g.sw;
+    const int s = A.sign;
+
+    for (int it = threadIdx.x; it < nrows * M2; it += blockDim.x) {
+        const int r = it / M2, j2 = it - r * M2;
+        const C* src = A.in + row0 + (i64)r * g.su + j2;
+        C v[M1];
+#pragma unroll
+        for (int j1 = 0; j1 < M1; ++j1) v[j1] = src[M2 * j1];
+        dftc<R, M1>(v, s);
+        int e = 0;
+#pragma unroll
+        for (int k1 = 1; k1 < M1; ++k1) {
+            e += j2;
+            if (e >= M) e -= M;
+            C t = __ldg(&A.tw[e]);
+            if (s > 0) t.y = -t.y;
+            v[k1] = cmul(v[k1], t);
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < M1; ++k1) ys[(k1 * M2 + j2) * P + r] = v[k1];
+    }
+    __syncthreads();
+    const FSeg* sg = A.segs + g.seg_first;
+    for (int it = threadIdx.x; it < nrows * M1; it += blockDim.x) {
+        const int k1 = it / nrows, r = it - k1 * nrows;
+        C u[M2];
+#pragma unroll
+        for (int j2 = 0; j2 < M2; ++j2) u[j2] = ys[(k1 * M2 + j2) * P + r];
+        dftc<R, M2>(u, s);
+        int q = 0;   // segment of point i (segments ascend in i and cover the row)
+        int i0 = sg[0].i0, i1 = sg[0].i1;
+        i64 base = sg[0].dst_off + (i64)w * sg[0].dw + u0 + r, di = sg[0].di;
+#pragma unroll
+        for (int k2 = 0; k2 < M2; ++k2) {
+            const int i = k1 + M1 * k2;
+            while (i >= i1 && q + 1 < g.nseg) {
+                ++q;
+                i0 = sg[q].i0; i1 = sg[q].i1;
+                base = sg[q].dst_off + (i64)w * sg[q].dw + u0 + r;
+                di = sg[q].di;
+            }
+            A.out[base + (i64)(i - i0) * di] = u[k2];
+        }
+    }
+}
+
+// Shared memory of a fused tile of S rows.
+inline size_t f2x_smem(int m1, int m2, int S, size_t es) { return (size_t)m1 * m2 * (S | 1) * es; }
+
+// Compiled fused kernels: float, core lengths of the C2C units; nullptr if none.
+void* f2_xpose_kernel_f32(int m, int* m1, int* m2);
+
 // Shared memory of a CTA of `per` signals.
 inline size_t f2_smem(int m1, int m2, bool cols, int per, size_t es, int mode) {
     if (cols) return (size_t)m1 * m2 * per * es;

@@ -1,5 +1,6 @@
-// Two-factor FFT kernels (fft_2f.cuh), float C2C rows and columns, lengths
-// 300..400: the most balanced split m = M1 * M2 with both factors at most 49.
+// Two-factor FFT kernels (fft_2f.cuh), float C2C rows and columns and the fused
+// rows + box-list transpose, lengths 300..400: the most balanced split
+// m = M1 * M2 with both factors at most 49.
 #include "fft_2f.cuh"
 
 namespace gb {
@@ -27,6 +28,30 @@ void* f2_kernel_f32_d(int m, bool cols, int mode, int* m1, int* m2) {
     GB_F2(400, 20, 20)
     }
 #undef GB_F2
+    return nullptr;
+}
+
+void* f2_xpose_kernel_f32_d(int m, int* m1, int* m2) {
+#define GB_F2X(M_, A_, B_)                                                                       \
+    case M_:                                                                                    \
+        *m1 = A_; *m2 = B_;                                                                     \
+        return (void*)fft2f_xpose_kernel<float, A_, B_>;
+    switch (m) {
+    GB_F2X(300, 15, 20)
+    GB_F2X(315, 15, 21)
+    GB_F2X(320, 16, 20)
+    GB_F2X(324, 18, 18)
+    GB_F2X(336, 16, 21)
+    GB_F2X(343, 7, 49)
+    GB_F2X(350, 14, 25)
+    GB_F2X(360, 18, 20)
+    GB_F2X(375, 15, 25)
+    GB_F2X(378, 18, 21)
+    GB_F2X(384, 16, 24)
+    GB_F2X(392, 14, 28)
+    GB_F2X(400, 20, 20)
+    }
+#undef GB_F2X
     return nullptr;
 }
 

@@ -1233,12 +1233,22 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
         }
     }
     const bool tile = aligned && tile_shape(m, dbl, true, ts, box_rows);
-    if (tile_only && !tile) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
+    // otherwise the two-factor kernel fused with the transpose (float) when one
+    // is compiled for m, else the register kernels
+    int f2a = 0, f2b = 0;
+    void* f2fn = nullptr;
+    {
+        const char* e = getenv("DTFFT_GB_F2");
+        if (!tile && !dbl && !(e && strcmp(e, "0") == 0)) f2fn = f2_xpose_kernel_f32(m, &f2a, &f2b);
+    }
+    if (tile_only && !tile && !f2fn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     int E = 0, T = 0;
     Schedule sch;
     int S = 1;
     if (tile) {
         S = ts.S;
+    } else if (f2fn) {
+        S = 8;   // rows per tile: runs of 8 adjacent destination points per output
     } else {
         if (!make_reg_schedule(m, false, E, sch, T, 64) && !make_reg_schedule(m, false, E, sch, T, 256))
             return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
@@ -1366,7 +1376,7 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
             }
             cudaGetLastError();
         }
-    } else {
+    } else if (!f2fn) {
         const int pitch = m + m / 16;
         p->pitch_ = pitch;
         p->smem_ = std::max((size_t)S * pitch, (size_t)m * (S + 1)) * es;
@@ -1376,6 +1386,12 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
             p->pipe_per_sm_ = pipe_occupancy(dbl, m, E, true, S * T, p->pipe_smem_);
         }
         err = upload_table(table_exp(m, 1, m), dbl, p->owned_, &p->tw_);
+    } else if (f2fn) {
+        p->f2_ = f2fn;
+        p->f2_threads_ = 128;
+        p->smem_ = f2x_smem(f2a, f2b, S, es);
+        err = set_smem_attrs(f2fn, p->smem_);
+        if (err == DTFFT_SUCCESS) err = upload_table(table_exp(m, 1, m), dbl, p->owned_, &p->tw_);
     }
     if (err == DTFFT_SUCCESS) {
         void* dg = nullptr; void* ds = nullptr;
@@ -1395,7 +1411,7 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
         err = status_setup();
     }
     if (err == DTFFT_SUCCESS) {
-        if (!tile)
+        if (!tile && !f2fn)
             err = set_smem_attrs(dbl ? (const void*)KPtr<double>::xpose(E) : (const void*)KPtr<float>::xpose(E),
                                  p->smem_);
     }
@@ -1635,6 +1651,19 @@ dtfft_error_t FusedFT::autotune(i64 max_elems, cudaStream_t s, int warmup, int i
 
 dtfft_error_t FusedFT::execute(const void* in, void* out, int sign, cudaStream_t s) {
     if (ctas_ == 0) return DTFFT_SUCCESS;
+    if (f2_) {
+        F2XArgs<float> A;
+        A.in = (const float2*)in; A.out = (float2*)out; A.tw = (const float2*)tw_;
+        A.groups = (const FGroup*)groups_; A.segs = (const FSeg*)segs_; A.ngroups = ngroups_;
+        A.S = S_; A.sign = sign;
+        void (*kfn)(F2XArgs<float>) = (void (*)(F2XArgs<float>))f2_;
+        void* tok = prof_begin(s);
+        kfn<<<(unsigned)ctas_, f2_threads_, smem_, s>>>(A);
+        if (tok) prof_end(tok, std::string("fft2f_xpose_m") + std::to_string(m_) + "_f32", s);
+        count_launch();
+        GB_CUDA_TRY(cudaGetLastError());
+        return DTFFT_SUCCESS;
+    }
     if (tile_) {
         if (((uintptr_t)in % 16) != 0 || ((uintptr_t)out % 16) != 0) return DTFFT_ERROR_INVALID_USAGE;
         const void* tw = sign > 0 ? tw_bwd_ : tw_;

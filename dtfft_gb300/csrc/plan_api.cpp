@@ -222,9 +222,10 @@ static dtfft_error_t build_ffts(Plan& p) {
 static dtfft_error_t build_fused(Plan& p) {
     if (p.transpose_only || p.kind == K_R2R || p.y_slab) return DTFFT_SUCCESS;
     if (p.z_slab && (p.kind == K_R2R || p.reshape || p.ndims != 3)) return DTFFT_SUCCESS;
-    // Default: fuse where the warp-per-row tile kernel takes the rows (it beats
-    // FFT + transpose there).  DTFFT_GB_FUSE=1 also fuses the other lengths
-    // with the register kernels; DTFFT_GB_FUSE=0 keeps every step unfused.
+    // Default: fuse where the warp-per-row tile kernel or (float) the
+    // two-factor kernel takes the rows (they beat FFT + transpose there).
+    // DTFFT_GB_FUSE=1 also fuses the other lengths with the register kernels;
+    // DTFFT_GB_FUSE=0 keeps every step unfused.
     // The tensor-core form (fft_form() == 1) keeps its row passes unfused.
     const char* fz = getenv("DTFFT_GB_FUSE");
     if ((fz && strcmp(fz, "0") == 0) || fft_form() == 1) return DTFFT_SUCCESS;

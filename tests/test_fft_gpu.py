@@ -268,11 +268,48 @@ def test_two_factor_real_rows(dt, cuda, monkeypatch, n, howmany):
     assert L.gb_fft_destroy(ctypes.byref(h)) == 0
 
 
+@pytest.mark.parametrize("kind,dims,grid", [
+    ("c2c", [105, 84, 60], [1, 2, 2]),     # every pass fused: X (105), Y (84) rows + transposes
+    ("c2c", [378, 45, 49], [1, 2, 1]),     # 45 rows per Y pencil split over 2: ragged 8-row tiles
+    ("c2c", [64, 105, 40], [1, 1, 1]),     # Z-slab plan on the generic X -> Y -> Z route
+    ("c2c", [225, 288, 49], [1, 1, 1]),    # the batch's first shape
+    ("r2c", [48, 175, 56], [1, 2, 2]),     # R2C: the complex Y / Z passes fuse
+    ("c2c", [49, 343, 7], [1, 3, 1]),      # three ranks, a 7-point Z axis that stays unfused
+])
+def test_two_factor_fused_transpose(dt, orc, cuda, kind, dims, grid):
+    """The two-factor kernel fused with the box-list transpose (default for
+    float lengths without a tile kernel): launch list and oracle parity."""
+    L = dt.lib()
+    np_dtype = np.complex64 if kind == "c2c" else np.float32
+    mk = dt.PlanC2C if kind == "c2c" else dt.PlanR2C
+    plan = mk(dims, comm=comm_for(dt, grid), precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT)
+    g = random_global(tuple(dims[::-1]), np_dtype, seed=47)
+    x = orc.global_to_packed(g, 3, grid, 1)
+    a = to_dev(x, plan.alloc_size, cuda)
+    b = empty(plan.alloc_size, np.complex64, cuda)
+    expect = orc.global_to_packed(orc.forward_values(g, kind), 3, grid, _final_layout(plan, 3))
+    L.dtfft_gb_profile_start()
+    plan.execute(a, b, dt.Execute.FORWARD)
+    fwd = from_dev(b, expect.size, np.complex64)
+    c = empty(plan.alloc_size, np_dtype, cuda)
+    plan.execute(b, c, dt.Execute.BACKWARD)
+    L.dtfft_gb_profile_stop()
+    names = _profiled_names(L)
+    assert any(nm.startswith("fft2f_xpose_m") for nm in names), names
+    assert L.dtfft_gb_device_status(1) == 0
+    assert orc.rel_l2(fwd, expect) <= 1e-5
+    back = from_dev(c, x.size, np_dtype).astype(np.complex128) / np.prod(dims)
+    assert orc.rel_l2(back, x) <= 1e-5
+    plan.destroy()
+
+
 @pytest.mark.parametrize("kind,dims", [("c2c", [64, 105, 40]), ("c2c", [75, 378, 49]), ("r2c", [48, 175, 56]),
                                        ("c2c", [50, 343, 40])])
 def test_two_factor_columns_in_z_slab_plans(dt, orc, cuda, monkeypatch, kind, dims):
-    """Z-slab plans whose Y columns (and X / Z rows) take the two-factor kernel."""
+    """Z-slab plans whose Y columns (and X / Z rows) take the two-factor kernel
+    (unfused: with fusion these plans take the generic X -> Y -> Z route)."""
     monkeypatch.setenv("DTFFT_GB_F2", "1")
+    monkeypatch.setenv("DTFFT_GB_FUSE", "0")
     L = dt.lib()
     np_dtype = np.complex64 if kind == "c2c" else np.float32
     mk = dt.PlanC2C if kind == "c2c" else dt.PlanR2C
