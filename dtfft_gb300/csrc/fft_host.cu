@@ -1248,7 +1248,10 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
     if (tile) {
         S = ts.S;
     } else if (f2fn) {
-        S = 8;   // rows per tile: runs of 8 adjacent destination points per output
+        // rows per tile (runs of S adjacent destination points per output):
+        // measured 3-8 % faster with 16 below 320 points, 8 above
+        S = m < 320 ? 16 : 8;
+        if (const char* e = getenv("DTFFT_GB_F2X_S")) S = std::min(32, std::max(1, atoi(e)));   // measurements
     } else {
         if (!make_reg_schedule(m, false, E, sch, T, 64) && !make_reg_schedule(m, false, E, sch, T, 256))
             return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
@@ -1389,6 +1392,10 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
     } else if (f2fn) {
         p->f2_ = f2fn;
         p->f2_threads_ = 128;
+        if (const char* e = getenv("DTFFT_GB_F2X_THREADS")) {   // measurements
+            const int t = atoi(e);
+            if (t == 32 || t == 64 || t == 256) p->f2_threads_ = t;
+        }
         p->smem_ = f2x_smem(f2a, f2b, S, es);
         err = set_smem_attrs(f2fn, p->smem_);
         if (err == DTFFT_SUCCESS) err = upload_table(table_exp(m, 1, m), dbl, p->owned_, &p->tw_);
