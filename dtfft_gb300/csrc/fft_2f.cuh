@@ -314,6 +314,127 @@ __global__ void __launch_bounds__(256) fft2f_xpose_kernel(const F2XArgs<R> A) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined rows (contiguous C2C rows, idist = odist = m): persistent CTAs
+// stream tiles of `per` rows into a ring of NST shared-memory buffers with
+// one cp.async.bulk each (transaction-count mbarriers, bounded waits), so the
+// loads of the next tiles are in flight while a tile is transformed; phase A
+// reads its points from the buffer instead of global memory.  `per` is even,
+// so every tile but the last starts 16-byte aligned; an odd tail of the last
+// tile (odd m, odd rows) is read with a plain load.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct F2PArgs {
+    typedef typename CT<R>::T C;
+    const C* in;
+    C* out;
+    const C* tw;
+    i64 nsig, ntiles;
+    int per, nst, sign, wait_limit;
+    int* status;
+};
+
+template <typename R, int M1, int M2>
+__device__ __forceinline__ void f2p_issue(const F2PArgs<R>& A, i64 t, typename CT<R>::T* buf, uint64_t* bar) {
+    constexpr int M = M1 * M2;
+    const i64 r0 = t * A.per;
+    const int nrows = (int)min((i64)A.per, A.nsig - r0);
+    const uint32_t elems = (uint32_t)nrows * M;
+    const uint32_t bytes = (elems & ~1u) * (uint32_t)sizeof(typename CT<R>::T);   // 16-byte multiple
+    mbar_expect_tx(bar, bytes);
+    bulk_load(buf, A.in + r0 * M, bytes, bar);
+}
+
+template <typename R, int M1, int M2>
+__global__ void __launch_bounds__(256) fft2f_pipe_kernel(const F2PArgs<R> A) {
+    typedef typename CT<R>::T C;
+    constexpr int M = M1 * M2;
+    constexpr int PR = M2 | 1;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+    const int per = A.per, NST = A.nst, s = A.sign;
+    C* inbuf = reinterpret_cast<C*>(smem_raw + 128);
+    C* ys = inbuf + (size_t)NST * per * M;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < NST; ++b) mbar_init(&bars[b], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int j = 0; j < NST; ++j) {
+            const i64 tj = blockIdx.x + (i64)j * gridDim.x;
+            if (tj < A.ntiles) f2p_issue<R, M1, M2>(A, tj, inbuf + (size_t)j * per * M, &bars[j]);
+        }
+    }
+    __syncthreads();
+    int k = 0;
+    for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x, ++k) {
+        const int b = k % NST;
+        const uint32_t par = (uint32_t)((k / NST) & 1);
+        const bool ok = mbar_wait_limit(&bars[b], par, A.wait_limit);
+        if (__syncthreads_or(!ok)) {
+            // give up: record, drain this CTA's copies still in flight, leave
+            if (threadIdx.x == 0) {
+                report_status(A.status, 1);
+                for (int j = 0; j < NST; ++j) {
+                    const i64 tj = tile + (i64)j * gridDim.x;
+                    if (tj >= A.ntiles) break;
+                    mbar_wait_bounded(&bars[(k + j) % NST], (uint32_t)(((k + j) / NST) & 1));
+                }
+            }
+            __syncthreads();
+            return;
+        }
+        const i64 r0 = tile * per;
+        const int nrows = (int)min((i64)per, A.nsig - r0);
+        C* buf = inbuf + (size_t)b * per * M;
+        if ((nrows * M) & 1) {   // odd tail of the last tile
+            if (threadIdx.x == 0) buf[nrows * M - 1] = A.in[r0 * M + nrows * M - 1];
+            __syncthreads();
+        }
+        for (int it = threadIdx.x; it < nrows * M2; it += blockDim.x) {
+            const int r = it / M2, j2 = it - r * M2;
+            const C* src = buf + r * M + j2;
+            C v[M1];
+#pragma unroll
+            for (int j1 = 0; j1 < M1; ++j1) v[j1] = src[M2 * j1];
+            dftc<R, M1>(v, s);
+            int e = 0;
+#pragma unroll
+            for (int k1 = 1; k1 < M1; ++k1) {
+                e += j2;
+                if (e >= M) e -= M;
+                C w = __ldg(&A.tw[e]);
+                if (s > 0) w.y = -w.y;
+                v[k1] = cmul(v[k1], w);
+            }
+#pragma unroll
+            for (int k1 = 0; k1 < M1; ++k1) ys[(r * M1 + k1) * PR + j2] = v[k1];
+        }
+        __syncthreads();   // buffer b read: refill it with tile + NST * grid
+        if (threadIdx.x == 0) {
+            fence_async_smem();
+            const i64 tn = tile + (i64)NST * gridDim.x;
+            if (tn < A.ntiles) f2p_issue<R, M1, M2>(A, tn, buf, &bars[b]);
+        }
+        for (int it = threadIdx.x; it < nrows * M1; it += blockDim.x) {
+            const int r = it / M1, k1 = it - r * M1;
+            C u[M2];
+#pragma unroll
+            for (int j2 = 0; j2 < M2; ++j2) u[j2] = ys[(r * M1 + k1) * PR + j2];
+            dftc<R, M2>(u, s);
+            C* dst = A.out + (r0 + r) * M + k1;
+#pragma unroll
+            for (int k2 = 0; k2 < M2; ++k2) dst[M1 * k2] = u[k2];
+        }
+        __syncthreads();   // the intermediate is rewritten by the next tile
+    }
+}
+
+inline size_t f2p_smem(int m1, int m2, int per, int nst, size_t es) {
+    return 128 + (size_t)nst * per * m1 * m2 * es + (size_t)per * m1 * (m2 | 1) * es;
+}
+
+// Compiled pipelined kernels: float, the lengths of the C2C units; nullptr if none.
+void* f2_pipe_kernel_f32(int m, int* m1, int* m2);
+
 // Shared memory of a fused tile of S rows.
 inline size_t f2x_smem(int m1, int m2, int S, size_t es) { return (size_t)m1 * m2 * (S | 1) * es; }
 

@@ -1,5 +1,5 @@
-// Two-factor FFT kernels (fft_2f.cuh), float C2C rows and columns and the fused
-// rows + box-list transpose, lengths 40..100: the most balanced split
+// Two-factor FFT kernels (fft_2f.cuh), float C2C rows and columns, pipelined
+// rows and the fused rows + box-list transpose, lengths 40..100: the most balanced split
 // m = M1 * M2 with both factors at most 49.
 #include "fft_2f.cuh"
 
@@ -71,6 +71,38 @@ void* f2_xpose_kernel_f32_a(int m, int* m1, int* m2) {
     return nullptr;
 }
 
+void* f2_pipe_kernel_f32_a(int m, int* m1, int* m2) {
+#define GB_F2P(M_, A_, B_)                                                                       \
+    case M_:                                                                                    \
+        *m1 = A_; *m2 = B_;                                                                     \
+        return (void*)fft2f_pipe_kernel<float, A_, B_>;
+    switch (m) {
+    GB_F2P(40, 5, 8)
+    GB_F2P(42, 6, 7)
+    GB_F2P(45, 5, 9)
+    GB_F2P(48, 6, 8)
+    GB_F2P(49, 7, 7)
+    GB_F2P(50, 5, 10)
+    GB_F2P(54, 6, 9)
+    GB_F2P(56, 7, 8)
+    GB_F2P(60, 6, 10)
+    GB_F2P(63, 7, 9)
+    GB_F2P(64, 8, 8)
+    GB_F2P(70, 7, 10)
+    GB_F2P(72, 8, 9)
+    GB_F2P(75, 5, 15)
+    GB_F2P(80, 8, 10)
+    GB_F2P(81, 9, 9)
+    GB_F2P(84, 7, 12)
+    GB_F2P(90, 9, 10)
+    GB_F2P(96, 8, 12)
+    GB_F2P(98, 7, 14)
+    GB_F2P(100, 10, 10)
+    }
+#undef GB_F2P
+    return nullptr;
+}
+
 void* f2_kernel_f32_b(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_kernel_f32_c(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_kernel_f32_d(int m, bool cols, int mode, int* m1, int* m2);
@@ -79,6 +111,9 @@ void* f2_kernel_f32_b_real(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_kernel_f32_c_real(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_kernel_f32_d_real(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_xpose_kernel_f32_b(int m, int* m1, int* m2);
+void* f2_pipe_kernel_f32_b(int m, int* m1, int* m2);
+void* f2_pipe_kernel_f32_c(int m, int* m1, int* m2);
+void* f2_pipe_kernel_f32_d(int m, int* m1, int* m2);
 void* f2_xpose_kernel_f32_c(int m, int* m1, int* m2);
 void* f2_xpose_kernel_f32_d(int m, int* m1, int* m2);
 
@@ -99,6 +134,18 @@ void* f2_xpose_kernel_f32(int m, int* m1, int* m2) {
     typedef void* (*Fn)(int, int*, int*);
     static const Fn units[4] = {f2_xpose_kernel_f32_a, f2_xpose_kernel_f32_b, f2_xpose_kernel_f32_c,
                                 f2_xpose_kernel_f32_d};
+    int a = 0, b = 0;
+    void* k = nullptr;
+    for (int i = 0; i < 4 && !k; ++i) k = units[i](m, &a, &b);
+    if (m1) *m1 = a;
+    if (m2) *m2 = b;
+    return k;
+}
+
+void* f2_pipe_kernel_f32(int m, int* m1, int* m2) {
+    typedef void* (*Fn)(int, int*, int*);
+    static const Fn units[4] = {f2_pipe_kernel_f32_a, f2_pipe_kernel_f32_b, f2_pipe_kernel_f32_c,
+                                f2_pipe_kernel_f32_d};
     int a = 0, b = 0;
     void* k = nullptr;
     for (int i = 0; i < 4 && !k; ++i) k = units[i](m, &a, &b);

@@ -1,5 +1,5 @@
-// Two-factor FFT kernels (fft_2f.cuh), float C2C rows and columns and the fused
-// rows + box-list transpose, lengths 105..196: the most balanced split
+// Two-factor FFT kernels (fft_2f.cuh), float C2C rows and columns, pipelined
+// rows and the fused rows + box-list transpose, lengths 105..196: the most balanced split
 // m = M1 * M2 with both factors at most 49.
 #include "fft_2f.cuh"
 
@@ -66,6 +66,37 @@ void* f2_xpose_kernel_f32_b(int m, int* m1, int* m2) {
     GB_F2X(196, 14, 14)
     }
 #undef GB_F2X
+    return nullptr;
+}
+
+void* f2_pipe_kernel_f32_b(int m, int* m1, int* m2) {
+#define GB_F2P(M_, A_, B_)                                                                       \
+    case M_:                                                                                    \
+        *m1 = A_; *m2 = B_;                                                                     \
+        return (void*)fft2f_pipe_kernel<float, A_, B_>;
+    switch (m) {
+    GB_F2P(105, 7, 15)
+    GB_F2P(108, 9, 12)
+    GB_F2P(112, 8, 14)
+    GB_F2P(120, 10, 12)
+    GB_F2P(125, 5, 25)
+    GB_F2P(126, 9, 14)
+    GB_F2P(128, 8, 16)
+    GB_F2P(135, 9, 15)
+    GB_F2P(140, 10, 14)
+    GB_F2P(144, 12, 12)
+    GB_F2P(147, 7, 21)
+    GB_F2P(150, 10, 15)
+    GB_F2P(160, 10, 16)
+    GB_F2P(162, 9, 18)
+    GB_F2P(168, 12, 14)
+    GB_F2P(175, 7, 25)
+    GB_F2P(180, 12, 15)
+    GB_F2P(189, 9, 21)
+    GB_F2P(192, 12, 16)
+    GB_F2P(196, 14, 14)
+    }
+#undef GB_F2P
     return nullptr;
 }
 

@@ -1,5 +1,5 @@
-// Two-factor FFT kernels (fft_2f.cuh), float C2C rows and columns and the fused
-// rows + box-list transpose, lengths 300..400: the most balanced split
+// Two-factor FFT kernels (fft_2f.cuh), float C2C rows and columns, pipelined
+// rows and the fused rows + box-list transpose, lengths 300..400: the most balanced split
 // m = M1 * M2 with both factors at most 49.
 #include "fft_2f.cuh"
 
@@ -52,6 +52,30 @@ void* f2_xpose_kernel_f32_d(int m, int* m1, int* m2) {
     GB_F2X(400, 20, 20)
     }
 #undef GB_F2X
+    return nullptr;
+}
+
+void* f2_pipe_kernel_f32_d(int m, int* m1, int* m2) {
+#define GB_F2P(M_, A_, B_)                                                                       \
+    case M_:                                                                                    \
+        *m1 = A_; *m2 = B_;                                                                     \
+        return (void*)fft2f_pipe_kernel<float, A_, B_>;
+    switch (m) {
+    GB_F2P(300, 15, 20)
+    GB_F2P(315, 15, 21)
+    GB_F2P(320, 16, 20)
+    GB_F2P(324, 18, 18)
+    GB_F2P(336, 16, 21)
+    GB_F2P(343, 7, 49)
+    GB_F2P(350, 14, 25)
+    GB_F2P(360, 18, 20)
+    GB_F2P(375, 15, 25)
+    GB_F2P(378, 18, 21)
+    GB_F2P(384, 16, 24)
+    GB_F2P(392, 14, 28)
+    GB_F2P(400, 20, 20)
+    }
+#undef GB_F2P
     return nullptr;
 }
 

@@ -132,6 +132,13 @@ struct FftStep {
     void* f2 = nullptr;      // C2C float: two-factor kernel (fft_2f.cuh), f2_m1 x f2_m2, f2_per signals per CTA
     int f2_m1 = 0, f2_m2 = 0, f2_per = 0, f2_threads = 256;
     size_t f2_smem = 0;
+    // pipelined form of the two-factor rows (fft2f_pipe_kernel): f2 is that kernel, with a ring of
+    // f2_nst buffers and at most f2_ctas CTAs per SM; f2_plain (f2_plain_per signals per CTA, 128
+    // threads) runs the rows when the input is not 16-byte aligned
+    bool f2_pipe = false;
+    int f2_nst = 2, f2_ctas = 0, f2_plain_per = 0;
+    void* f2_plain = nullptr;
+    size_t f2_plain_smem = 0;
     ~FftStep() { tc_destroy(tc); blue_destroy(blue); }
 };
 
@@ -524,17 +531,33 @@ static dtfft_error_t launch_pipe(const PArgs<R>& P, int E, int threads, size_t s
 template <typename R, bool COLS>
 static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, cudaStream_t s) {
     if (S.blue) return blue_execute(S.blue, in, out, s);
+    if (S.f2 && S.f2_pipe && ((uintptr_t)in % 16) == 0) {
+        F2PArgs<R> P;
+        P.in = (const typename CT<R>::T*)in; P.out = (typename CT<R>::T*)out; P.tw = (const typename CT<R>::T*)S.tw;
+        P.nsig = S.nsig; P.per = S.f2_per; P.ntiles = (S.nsig + S.f2_per - 1) / S.f2_per; P.nst = S.f2_nst;
+        P.sign = S.sign; P.wait_limit = g_wait_limit; P.status = status_ptr();
+        if (P.ntiles <= 0) return DTFFT_SUCCESS;
+        const i64 grid = std::min<i64>(P.ntiles, (i64)sm_count() * S.f2_ctas);
+        void (*kfn)(F2PArgs<R>) = (void (*)(F2PArgs<R>))S.f2;
+        void* tok = prof_begin(s);
+        kfn<<<(unsigned)grid, S.f2_threads, S.f2_smem, s>>>(P);
+        if (tok) prof_end(tok, std::string("fft2f_pipe_c2c_m") + std::to_string(S.m) + "_f32", s);
+        count_launch();
+        GB_CUDA_TRY(cudaGetLastError());
+        return DTFFT_SUCCESS;
+    }
     if (S.f2) {
+        const bool plain = S.f2_pipe;   // unaligned input of a pipelined step
         F2Args<R> F;
         F.in = in; F.out = out; F.tw = (const typename CT<R>::T*)S.tw; F.ta = (const typename CT<R>::T*)S.ta;
         F.n = S.n; F.nsig = S.nsig; F.idist = S.idist; F.odist = S.odist; F.plane = S.plane; F.ld = S.ld; F.ncols = S.ncols;
-        F.sign = S.sign; F.per = S.f2_per;
-        const i64 ctas = (S.nsig + S.f2_per - 1) / S.f2_per;
+        F.sign = S.sign; F.per = plain ? S.f2_plain_per : S.f2_per;
+        const i64 ctas = (S.nsig + F.per - 1) / F.per;
         if (ctas <= 0) return DTFFT_SUCCESS;
         if (ctas > 0x7fffffffLL) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
-        void (*kfn)(F2Args<R>) = (void (*)(F2Args<R>))S.f2;
+        void (*kfn)(F2Args<R>) = (void (*)(F2Args<R>))(plain ? S.f2_plain : S.f2);
         void* tok = prof_begin(s);
-        kfn<<<(unsigned)ctas, S.f2_threads, S.f2_smem, s>>>(F);
+        kfn<<<(unsigned)ctas, plain ? 128 : S.f2_threads, plain ? S.f2_plain_smem : S.f2_smem, s>>>(F);
         if (tok) {
             static const char* mn[] = {"c2c", "r2c", "r2c", "c2r", "c2r"};
             prof_end(tok, std::string("fft2f_") + (COLS ? "cols_" : "rows_") + mn[S.mode] + "_m" + std::to_string(S.m) +
@@ -744,7 +767,7 @@ dtfft_error_t FftPlan::execute(const void* in, void* out, int sign, cudaStream_t
 // fastest is kept.  Choices are cached per (GPU, library version, step
 // geometry) in the process and, with DTFFT_GB_TUNE_CACHE, in that file.
 struct StepCand {
-    enum Kind { TILE, PIPE, REG, SMEM, F2 } kind = SMEM;
+    enum Kind { TILE, PIPE, REG, SMEM, F2, F2P } kind = SMEM;
     int E = 0, per = 1, S = 0, nst = 0;
     std::vector<int> radix;
     std::string name() const {
@@ -753,6 +776,7 @@ struct StepCand {
         case TILE: o << "tile:S" << S << ":nst" << nst; break;
         case SMEM: o << "smem"; break;
         case F2: o << "f2:t" << S << ":per" << per; break;
+        case F2P: o << "f2p:t" << S << ":per" << per << ":nst" << nst; break;
         default: {
             o << (kind == PIPE ? "pipe:E" : "reg:E") << E << ":";
             for (size_t i = 0; i < radix.size(); ++i) o << (i ? "x" : "") << radix[i];
@@ -764,6 +788,11 @@ struct StepCand {
     static bool parse(const std::string& t, StepCand& c) {
         c = StepCand();
         if (t == "smem") { c.kind = SMEM; return true; }
+        if (t.compare(0, 4, "f2p:") == 0) {
+            c.kind = F2P;
+            return sscanf(t.c_str(), "f2p:t%d:per%d:nst%d", &c.S, &c.per, &c.nst) == 3 && c.per > 0 && c.per % 2 == 0 &&
+                   (c.S == 128 || c.S == 256) && c.nst >= 2 && c.nst <= 4;
+        }
         if (t.compare(0, 3, "f2:") == 0) {
             c.kind = F2;
             return sscanf(t.c_str(), "f2:t%d:per%d", &c.S, &c.per) == 2 && c.per > 0 &&
@@ -818,7 +847,31 @@ static bool apply_cand(FftStep& S, const StepCand& c, std::vector<void*>& owned)
     S.tile = false;
     S.pipe = false;
     S.f2 = nullptr;
+    S.f2_pipe = false;
+    S.f2_plain = nullptr;
     switch (c.kind) {
+    case StepCand::F2P: {
+        int a = 0, b = 0, pa = 0, pb = 0;
+        if (S.dbl || !c2c_rows || c.per < 2 || c.per % 2 || c.nst < 2 || c.nst > 4) return false;
+        void* fn = f2_pipe_kernel_f32(m, &a, &b);
+        void* plain = f2_kernel_f32(m, false, M_C2C, &pa, &pb);
+        if (!fn || !plain) return false;
+        const size_t smem = f2p_smem(a, b, c.per, c.nst, es);
+        const int threads = c.S == 128 ? 128 : 256;
+        if (smem > max_optin_smem() || set_smem_attrs(fn, smem) != DTFFT_SUCCESS) { cudaGetLastError(); return false; }
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem) != cudaSuccess || occ < 1) {
+            cudaGetLastError();
+            return false;
+        }
+        const int pper = std::max(1, (128 + std::min(pa, pb) - 1) / std::min(pa, pb) / 2);
+        const size_t psmem = f2_smem(pa, pb, false, pper, es, M_C2C);
+        if (set_smem_attrs(plain, psmem) != DTFFT_SUCCESS) { cudaGetLastError(); return false; }
+        S.f2 = fn; S.f2_m1 = a; S.f2_m2 = b; S.f2_per = c.per; S.f2_smem = smem; S.f2_threads = threads;
+        S.f2_pipe = true; S.f2_nst = c.nst; S.f2_ctas = occ;
+        S.f2_plain = plain; S.f2_plain_per = pper; S.f2_plain_smem = psmem;
+        return true;
+    }
     case StepCand::F2: {
         int a = 0, b = 0;
         void* fn = (S.dbl || S.mode > M_C2R_FULL) ? nullptr : f2_kernel_f32(m, S.cols, S.mode, &a, &b);
@@ -903,9 +956,10 @@ static bool apply_cand(FftStep& S, const StepCand& c, std::vector<void*>& owned)
 }
 
 // C2C, R2C and C2R float steps without a tile kernel take the two-factor
-// kernel when one is compiled for their core length (measured faster than the register, pipelined
-// and shared-memory kernels on most such lengths; EXHAUSTIVE plans time them
-// all).  DTFFT_GB_F2=0: never; DTFFT_GB_F2=1: also over the tile kernels.
+// kernel when one is compiled for their core length (measured faster than the
+// register, pipelined and shared-memory kernels on most such lengths;
+// EXHAUSTIVE plans time them all).  DTFFT_GB_F2=0: never; DTFFT_GB_F2=1: also
+// over the tile kernels.
 static void f2_prefer(FftStep& S, std::vector<void*>& owned) {
     const char* e = getenv("DTFFT_GB_F2");
     const bool never = e && strcmp(e, "0") == 0, always = e && strcmp(e, "1") == 0;
@@ -923,10 +977,27 @@ static void f2_prefer(FftStep& S, std::vector<void*>& owned) {
     }
     c.per = S.cols ? 32 : std::max(1, (c.S + std::min(a, b) - 1) / std::min(a, b) / 2);
     if (const char* v = getenv("DTFFT_GB_F2_PER")) c.per = std::max(1, atoi(v));
-    FftStep t = S;
-    t.tc = nullptr; t.blue = nullptr;
-    if (apply_cand(t, c, owned)) S = t;
-    t.tc = nullptr; t.blue = nullptr;
+    // contiguous C2C rows: the pipelined form, 128 threads, a ring of two tiles of about
+    // 1024 points (4-16 rows), measured 10-15 % faster than the unpipelined kernel
+    // (DTFFT_GB_F2P=0: the unpipelined kernel; "threads,per,nst": that shape, for measurements)
+    const bool c2c_rows = !S.cols && S.mode == M_C2C && S.idist == S.m && S.odist == S.m;
+    StepCand cp;
+    const char* pv = getenv("DTFFT_GB_F2P");
+    if (c2c_rows && !(pv && strcmp(pv, "0") == 0) && f2_pipe_kernel_f32(S.m, nullptr, nullptr)) {
+        cp.kind = StepCand::F2P; cp.S = 128; cp.nst = 2;
+        cp.per = 2 * std::max(2, std::min(8, (512 + S.m / 2) / S.m));
+        int nt = 0, per = 0, nst = 0;
+        if (pv && sscanf(pv, "%d,%d,%d", &nt, &per, &nst) == 3) { cp.S = nt; cp.per = per; cp.nst = nst; }
+    }
+    for (const StepCand& k : {cp, c}) {
+        if (k.kind != StepCand::F2P && k.kind != StepCand::F2) continue;
+        FftStep t = S;
+        t.tc = nullptr; t.blue = nullptr;
+        const bool ok = apply_cand(t, k, owned);
+        if (ok) S = t;
+        t.tc = nullptr; t.blue = nullptr;
+        if (ok) return;
+    }
 }
 
 static std::vector<StepCand> step_candidates(const FftStep& S) {
@@ -994,6 +1065,17 @@ static std::vector<StepCand> step_candidates(const FftStep& S) {
                 for (const StepCand& o : out) dup = dup || (o.kind == c.kind && o.per == c.per && o.S == c.S);
                 if (!dup) out.push_back(c);
             }
+        }
+        // pipelined rows: 128 or 256 threads, tiles of 4, 8 or 16 rows, rings of 2 or 3 tiles
+        if (c2c_rows && f2_pipe_kernel_f32(m, nullptr, nullptr)) {
+            for (int nt : {128, 256})
+                for (int per : {4, 8, 16})
+                    for (int nst : {2, 3}) {
+                        if (f2p_smem(a, b, per, nst, es) > 200 * 1024) continue;
+                        StepCand c;
+                        c.kind = StepCand::F2P; c.S = nt; c.per = per; c.nst = nst;
+                        out.push_back(c);
+                    }
         }
     }
     return out;

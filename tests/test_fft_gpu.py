@@ -132,6 +132,8 @@ def test_fused_fft_transpose(dt, orc, cuda, monkeypatch, dims, grid, np_dtype):
     ([256, 50, 36], [1, 2, 2], np.complex64, False),     # 25 rows per rank: ragged odd tiles, odd destinations
     ([512, 50, 36], [1, 2, 2], np.complex128, False),
     ([768, 24, 20], [1, 2, 1], np.complex64, False),     # store warps write straight from shared memory
+    ([105, 84, 60], [1, 2, 2], np.complex64, True),      # fused two-factor passes, in == out
+    ([225, 98, 45], [1, 1, 1], np.complex64, True),      # Z-slab on the two-factor generic route, in == out
 ])
 def test_tile_schedules(dt, orc, cuda, dims, grid, np_dtype, inplace):
     """Fused tile passes on the default path: Z-slab plans take the generic
@@ -210,6 +212,7 @@ def test_two_factor_rows(dt, cuda, monkeypatch, n, howmany):
     backward against numpy FP64, ragged last CTA included."""
     import torch
     monkeypatch.setenv("DTFFT_GB_F2", "1")
+    monkeypatch.setenv("DTFFT_GB_F2P", "0")      # the unpipelined kernel (pipelined rows: below)
     L = dt.lib()
     h = ctypes.c_void_p()
     sizes = (ctypes.c_int32 * 1)(n)
@@ -230,6 +233,44 @@ def test_two_factor_rows(dt, cuda, monkeypatch, n, howmany):
     ref = np.fft.fft(x.astype(np.complex128), axis=1)
     assert np.linalg.norm(fwd - ref) / np.linalg.norm(ref) <= 1e-5
     back = a.cpu().numpy() / n
+    assert np.linalg.norm(back - x) / np.linalg.norm(x) <= 1e-5
+    assert L.gb_fft_destroy(ctypes.byref(h)) == 0
+
+
+@pytest.mark.parametrize("n,howmany,shape", [(105, 777, "256,8,2"), (378, 301, "128,4,3"), (225, 1000, "256,16,2"),
+                                              (343, 99, "128,16,3"), (40, 5001, "256,4,2")])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_two_factor_pipelined_rows(dt, cuda, monkeypatch, n, howmany, shape, offset):
+    """Pipelined two-factor rows (bulk-copy ring of row tiles): odd lengths
+    with an odd last tile (the 8-byte tail read apart), and an input one
+    element off 16-byte alignment, which runs the unpipelined kernel."""
+    import torch
+    monkeypatch.setenv("DTFFT_GB_F2P", shape)
+    L = dt.lib()
+    h = ctypes.c_void_p()
+    sizes = (ctypes.c_int32 * 1)(n)
+    assert L.gb_fft_create(1, 0, 0, n, n, howmany, sizes, sizes, sizes, None, None, ctypes.byref(h)) == 0
+    rng = np.random.default_rng(n + offset)
+    x = (rng.uniform(-1, 1, (howmany, n)) + 1j * rng.uniform(-1, 1, (howmany, n))).astype(np.complex64)
+    buf = torch.zeros(howmany * n + 2, dtype=torch.complex64, device=cuda)
+    a = buf[offset:offset + howmany * n]
+    a.copy_(torch.from_numpy(x.ravel()).to(cuda))
+    b = torch.empty(howmany * n, dtype=torch.complex64, device=cuda)
+    torch.cuda.synchronize()
+    L.dtfft_gb_profile_start()
+    assert L.gb_fft_execute(h, a.data_ptr(), b.data_ptr(), -1) == 0
+    torch.cuda.synchronize()
+    L.dtfft_gb_profile_stop()
+    names = _profiled_names(L)
+    want = ("fft2f_rows_c2c_m%d_f32" if offset else "fft2f_pipe_c2c_m%d_f32") % n
+    assert want in names, names
+    assert L.dtfft_gb_device_status(1) == 0
+    fwd = b.cpu().numpy().reshape(howmany, n)
+    ref = np.fft.fft(x.astype(np.complex128), axis=1)
+    assert np.linalg.norm(fwd - ref) / np.linalg.norm(ref) <= 1e-5
+    assert L.gb_fft_execute(h, b.data_ptr(), a.data_ptr(), 1) == 0
+    torch.cuda.synchronize()
+    back = a.cpu().numpy().reshape(howmany, n) / n
     assert np.linalg.norm(back - x) / np.linalg.norm(x) <= 1e-5
     assert L.gb_fft_destroy(ctypes.byref(h)) == 0
 

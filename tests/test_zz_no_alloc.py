@@ -12,7 +12,7 @@ more scratch than the buffer are refused.
 
 Cases: out-of-place and in-place generic C2C, a plan whose X and Y passes run
 the fused tile FFT + transpose kernel, a transpose-only plan (TMA transposes),
-R2C, R2R and a Z-slab plan.
+R2C, R2R, a Z-slab plan and a plan on the fused two-factor passes.
 
 This file is collected last so that a run stopping at the first failure has
 already run every other test; it also passes alone in a fresh process.
@@ -65,6 +65,8 @@ def _make(dt, case):
                            executor=dt.Executor.VKFFT), np.float64, np.float64)
     if case == "z_slab":
         return dt.PlanC2C([64, 48, 40], precision=S, executor=dt.Executor.CUFFT), np.complex64, np.complex64
+    if case == "two_factor_fused":
+        return dt.PlanC2C([105, 42, 36], comm=g22, precision=S, executor=dt.Executor.CUFFT), np.complex64, np.complex64
     raise ValueError(case)
 
 
@@ -75,7 +77,8 @@ def _random(n, np_dtype, seed):
     return rng.uniform(-1, 1, n).astype(np_dtype)
 
 
-@pytest.mark.parametrize("case", ["c2c", "c2c_inplace", "c2c_fused_tile", "transpose_only", "r2c", "r2r", "z_slab"])
+@pytest.mark.parametrize("case", ["c2c", "c2c_inplace", "c2c_fused_tile", "transpose_only", "r2c", "r2r", "z_slab",
+                                  "two_factor_fused"])
 def test_noalloc_matches_execute_bit_for_bit(dt, cuda, case):
     import torch
     from tests.gpu_util import torch_dtype
