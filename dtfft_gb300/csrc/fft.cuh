@@ -114,6 +114,7 @@ private:
     // warp-per-row tile kernel (fft_tile.cuh): used when tile_ is set
     bool tile_ = false;
     int tile_nst_ = 0, tile_threads_ = 0, pair_ok_ = 0, ncw_ = 0, nsw_ = 0;
+    int wfast_ = 0;          // tile order of the pass: w first (1) or u first (0)
     const void* tw_bwd_ = nullptr;
     // tensor-store write-out of the tile pass (fft_tile_xpose_tma_kernel);
     // null when the pass's segments do not fit it or `use_xtma_` is off

@@ -583,6 +583,7 @@ static dtfft_error_t launch_step_t(const FftStep& S, const void* in, void* out, 
         P.nsig = S.nsig; P.groups = nullptr; P.segs = nullptr; P.ngroups = 0;
         P.ntiles = (S.nsig + S.tile_S - 1) / S.tile_S;
         P.S = S.tile_S; P.nst = S.tile_nst; P.pair_ok = 0; P.wait_limit = g_wait_limit; P.status = status_ptr();
+        P.wfast = 0;
         void (*kfn)(TArgs<R>) = (void (*)(TArgs<R>))TilePtr<R>::get(S.m, S.sign, false, S.tile_nw);
         if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
         const i64 grid = std::min<i64>(P.ntiles, (i64)sm_count());
@@ -1383,6 +1384,7 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
     dtfft_error_t err = DTFFT_SUCCESS;
     if (tile) {
         p->tile_ = true;
+        if (const char* e = getenv("DTFFT_GB_TILE_WFAST")) p->wfast_ = atoi(e) == 1;   // measurements
         p->tile_nst_ = ts.nst;
         p->tile_threads_ = ts.threads;
         p->smem_ = ts.smem;
@@ -1557,7 +1559,7 @@ static dtfft_error_t launch_fused_pipe(int m, int E, int T, int S, int pitch, co
 
 template <typename R>
 static dtfft_error_t launch_fused_tile_tma(int m, XTma& x, const void* tw, const void* groups, const void* segs,
-                                          int ngroups, i64 tiles, const void* in, void* out, int sign,
+                                          int ngroups, i64 tiles, const void* in, void* out, int sign, int wfast,
                                           cudaStream_t s) {
     typedef typename CT<R>::T C;
     TXArgs<R> X;
@@ -1568,6 +1570,7 @@ static dtfft_error_t launch_fused_tile_tma(int m, XTma& x, const void* tw, const
     if (x.dgroups) { P.groups = (const FGroup*)x.dgroups; tiles = x.tiles; }
     P.ntiles = tiles; P.S = x.S; P.nst = x.nst; P.pair_ok = 0; P.wait_limit = g_wait_limit;
     P.status = status_ptr();
+    P.wfast = wfast;
     {
         std::lock_guard<std::mutex> lk(x.mu);
         TmaXMaps* mp = nullptr;
@@ -1597,13 +1600,14 @@ static dtfft_error_t launch_fused_tile_tma(int m, XTma& x, const void* tw, const
 template <typename R>
 static dtfft_error_t launch_fused_tile(int m, int S, int nst, int threads, int ncw, int nsw, size_t smem, int pair_ok,
                                       const void* tw, const void* groups, const void* segs, int ngroups, i64 tiles,
-                                      const void* in, void* out, int sign, cudaStream_t s) {
+                                      const void* in, void* out, int sign, int wfast, cudaStream_t s) {
     typedef typename CT<R>::T C;
     TArgs<R> P;
     P.in = (const C*)in; P.out = (C*)out; P.tw = (const C*)tw;
     P.nsig = 0; P.groups = (const FGroup*)groups; P.segs = (const FSeg*)segs; P.ngroups = ngroups;
     P.ntiles = tiles; P.S = S; P.nst = nst; P.pair_ok = pair_ok; P.wait_limit = g_wait_limit;
     P.status = status_ptr();
+    P.wfast = wfast;
     void (*kfn)(TArgs<R>) = (void (*)(TArgs<R>))TilePtr<R>::get(m, sign, true, ncw, nsw);
     if (!kfn) return DTFFT_ERROR_FFT_SIZE_NOT_SUPPORTED;
     const i64 grid = std::min<i64>(tiles, (i64)sm_count());
@@ -1758,14 +1762,15 @@ dtfft_error_t FusedFT::execute(const void* in, void* out, int sign, cudaStream_t
         const void* tw = sign > 0 ? tw_bwd_ : tw_;
         if (use_xtma_ && xtma_) {
             if (dbl_)
-                return launch_fused_tile_tma<double>(m_, *xtma_, tw, groups_, segs_, ngroups_, ctas_, in, out, sign, s);
-            return launch_fused_tile_tma<float>(m_, *xtma_, tw, groups_, segs_, ngroups_, ctas_, in, out, sign, s);
+                return launch_fused_tile_tma<double>(m_, *xtma_, tw, groups_, segs_, ngroups_, ctas_, in, out, sign,
+                                                     wfast_, s);
+            return launch_fused_tile_tma<float>(m_, *xtma_, tw, groups_, segs_, ngroups_, ctas_, in, out, sign, wfast_, s);
         }
         if (dbl_)
             return launch_fused_tile<double>(m_, S_, tile_nst_, tile_threads_, ncw_, nsw_, smem_, pair_ok_, tw, groups_,
-                                             segs_, ngroups_, ctas_, in, out, sign, s);
+                                             segs_, ngroups_, ctas_, in, out, sign, wfast_, s);
         return launch_fused_tile<float>(m_, S_, tile_nst_, tile_threads_, ncw_, nsw_, smem_, pair_ok_, tw, groups_,
-                                        segs_, ngroups_, ctas_, in, out, sign, s);
+                                        segs_, ngroups_, ctas_, in, out, sign, wfast_, s);
     }
     if (pipe_per_sm_ > 0 && ((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0) {
         if (dbl_)

@@ -62,6 +62,7 @@ struct TArgs {
     int pair_ok;          // xpose, complex64: destinations allow 16-byte stores of two rows
     int wait_limit;       // iteration limit of the waits for a tile's bulk copy
     int* status;
+    int wfast;            // xpose: consecutive tiles of a block walk w first (else u first)
 };
 
 // Ring depth limit and the shared-memory header (mbarriers, flags) in front of
@@ -205,8 +206,13 @@ __device__ __forceinline__ void tile_geom(const TArgs<R>& A, i64 tile, i64& row0
         }
         const FGroup& g = A.groups[lo];
         const int tl = (int)(tile - g.cta_begin);
-        u0 = (tl % g.tiles_u) * A.S;
-        w = tl / g.tiles_u;
+        if (A.wfast) {
+            u0 = (tl / g.nw) * A.S;
+            w = tl % g.nw;
+        } else {
+            u0 = (tl % g.tiles_u) * A.S;
+            w = tl / g.tiles_u;
+        }
         nrows = min(A.S, g.nu - u0);
         row0 = g.src_off + (i64)u0 * g.su + (i64)w * g.sw;
         rs = g.su;
