@@ -547,7 +547,10 @@ def config1_section(args, dt, dev, stream):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / k
         out[name] = {"cycles_per_s": 1000.0 / ms, "ms_per_cycle": ms}
-    out["kernels_per_cycle"] = 2 * 3
+    l0 = dt.kernel_launches()
+    plain()
+    torch.cuda.synchronize()
+    out["kernels_per_cycle"] = dt.kernel_launches() - l0
     batch.destroy()
     plan.destroy()
     return out
