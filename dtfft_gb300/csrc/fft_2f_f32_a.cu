@@ -106,25 +106,34 @@ void* f2_pipe_kernel_f32_a(int m, int* m1, int* m2) {
 void* f2_kernel_f32_b(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_kernel_f32_c(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_kernel_f32_d(int m, bool cols, int mode, int* m1, int* m2);
+void* f2_kernel_f32_e(int m, bool cols, int mode, int* m1, int* m2);
+void* f2_kernel_f32_f(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_kernel_f32_a_real(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_kernel_f32_b_real(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_kernel_f32_c_real(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_kernel_f32_d_real(int m, bool cols, int mode, int* m1, int* m2);
+void* f2_kernel_f32_e_real(int m, bool cols, int mode, int* m1, int* m2);
+void* f2_kernel_f32_f_real(int m, bool cols, int mode, int* m1, int* m2);
 void* f2_xpose_kernel_f32_b(int m, int* m1, int* m2);
 void* f2_pipe_kernel_f32_b(int m, int* m1, int* m2);
 void* f2_pipe_kernel_f32_c(int m, int* m1, int* m2);
 void* f2_pipe_kernel_f32_d(int m, int* m1, int* m2);
+void* f2_pipe_kernel_f32_e(int m, int* m1, int* m2);
+void* f2_pipe_kernel_f32_f(int m, int* m1, int* m2);
 void* f2_xpose_kernel_f32_c(int m, int* m1, int* m2);
 void* f2_xpose_kernel_f32_d(int m, int* m1, int* m2);
+void* f2_xpose_kernel_f32_e(int m, int* m1, int* m2);
+void* f2_xpose_kernel_f32_f(int m, int* m1, int* m2);
 
 void* f2_kernel_f32(int m, bool cols, int mode, int* m1, int* m2) {
     typedef void* (*Fn)(int, bool, int, int*, int*);
-    static const Fn units[8] = {f2_kernel_f32_a, f2_kernel_f32_b, f2_kernel_f32_c, f2_kernel_f32_d,
-                                f2_kernel_f32_a_real, f2_kernel_f32_b_real, f2_kernel_f32_c_real,
-                                f2_kernel_f32_d_real};
+    static const Fn units[12] = {f2_kernel_f32_a,      f2_kernel_f32_b,      f2_kernel_f32_c,
+                                 f2_kernel_f32_d,      f2_kernel_f32_e,      f2_kernel_f32_f,
+                                 f2_kernel_f32_a_real, f2_kernel_f32_b_real, f2_kernel_f32_c_real,
+                                 f2_kernel_f32_d_real, f2_kernel_f32_e_real, f2_kernel_f32_f_real};
     int a = 0, b = 0;
     void* k = nullptr;
-    for (int i = 0; i < 8 && !k; ++i) k = units[i](m, cols, mode, &a, &b);
+    for (int i = 0; i < 12 && !k; ++i) k = units[i](m, cols, mode, &a, &b);
     if (m1) *m1 = a;
     if (m2) *m2 = b;
     return k;
@@ -132,11 +141,11 @@ void* f2_kernel_f32(int m, bool cols, int mode, int* m1, int* m2) {
 
 void* f2_xpose_kernel_f32(int m, int* m1, int* m2) {
     typedef void* (*Fn)(int, int*, int*);
-    static const Fn units[4] = {f2_xpose_kernel_f32_a, f2_xpose_kernel_f32_b, f2_xpose_kernel_f32_c,
-                                f2_xpose_kernel_f32_d};
+    static const Fn units[6] = {f2_xpose_kernel_f32_a, f2_xpose_kernel_f32_b, f2_xpose_kernel_f32_c,
+                                f2_xpose_kernel_f32_d, f2_xpose_kernel_f32_e, f2_xpose_kernel_f32_f};
     int a = 0, b = 0;
     void* k = nullptr;
-    for (int i = 0; i < 4 && !k; ++i) k = units[i](m, &a, &b);
+    for (int i = 0; i < 6 && !k; ++i) k = units[i](m, &a, &b);
     if (m1) *m1 = a;
     if (m2) *m2 = b;
     return k;
@@ -144,11 +153,11 @@ void* f2_xpose_kernel_f32(int m, int* m1, int* m2) {
 
 void* f2_pipe_kernel_f32(int m, int* m1, int* m2) {
     typedef void* (*Fn)(int, int*, int*);
-    static const Fn units[4] = {f2_pipe_kernel_f32_a, f2_pipe_kernel_f32_b, f2_pipe_kernel_f32_c,
-                                f2_pipe_kernel_f32_d};
+    static const Fn units[6] = {f2_pipe_kernel_f32_a, f2_pipe_kernel_f32_b, f2_pipe_kernel_f32_c,
+                                f2_pipe_kernel_f32_d, f2_pipe_kernel_f32_e, f2_pipe_kernel_f32_f};
     int a = 0, b = 0;
     void* k = nullptr;
-    for (int i = 0; i < 4 && !k; ++i) k = units[i](m, &a, &b);
+    for (int i = 0; i < 6 && !k; ++i) k = units[i](m, &a, &b);
     if (m1) *m1 = a;
     if (m2) *m2 = b;
     return k;

@@ -205,7 +205,7 @@ def test_tensor_store_fused_pass(dt, orc, cuda, monkeypatch, dims, grid):
 
 
 @pytest.mark.parametrize("n,howmany", [(105, 777), (378, 300), (225, 1001), (343, 100), (40, 5000), (400, 64),
-                                        (245, 3)])
+                                        (245, 3), (1000, 300), (882, 97), (729, 200), (405, 50)])
 def test_two_factor_rows(dt, cuda, monkeypatch, n, howmany):
     """Batched C2C rows on the two-factor kernel (fft_2f.cuh; DTFFT_GB_F2=1
     makes every C2C float step with a compiled split take it): forward and
@@ -238,7 +238,8 @@ def test_two_factor_rows(dt, cuda, monkeypatch, n, howmany):
 
 
 @pytest.mark.parametrize("n,howmany,shape", [(105, 777, "256,8,2"), (378, 301, "128,4,3"), (225, 1000, "256,16,2"),
-                                              (343, 99, "128,16,3"), (40, 5001, "256,4,2")])
+                                              (343, 99, "128,16,3"), (40, 5001, "256,4,2"), (1008, 63, "128,4,2"),
+                                              (945, 100, "256,2,2")])
 @pytest.mark.parametrize("offset", [0, 1])
 def test_two_factor_pipelined_rows(dt, cuda, monkeypatch, n, howmany, shape, offset):
     """Pipelined two-factor rows (bulk-copy ring of row tiles): odd lengths
@@ -275,7 +276,8 @@ def test_two_factor_pipelined_rows(dt, cuda, monkeypatch, n, howmany, shape, off
     assert L.gb_fft_destroy(ctypes.byref(h)) == 0
 
 
-@pytest.mark.parametrize("n,howmany", [(350, 513), (245, 77), (96, 1000), (756, 31), (125, 300), (80, 7)])
+@pytest.mark.parametrize("n,howmany", [(350, 513), (245, 77), (96, 1000), (756, 31), (125, 300), (80, 7),
+                                        (1400, 40), (945, 33), (2000, 9)])
 def test_two_factor_real_rows(dt, cuda, monkeypatch, n, howmany):
     """R2C / C2R rows on the two-factor kernel: even n through the n/2-point
     core (R2C pairs outputs k and n/2 - k in a third phase), odd n through the
@@ -316,6 +318,8 @@ def test_two_factor_real_rows(dt, cuda, monkeypatch, n, howmany):
     ("c2c", [225, 288, 49], [1, 1, 1]),    # the batch's first shape
     ("r2c", [48, 175, 56], [1, 2, 2]),     # R2C: the complex Y / Z passes fuse
     ("c2c", [49, 343, 7], [1, 3, 1]),      # three ranks, a 7-point Z axis that stays unfused
+    ("c2c", [1000, 60, 48], [1, 2, 2]),    # 1000 = 25 x 40
+    ("c2c", [42, 729, 40], [1, 1, 1]),     # Z-slab generic route with a 729-point Y axis
 ])
 def test_two_factor_fused_transpose(dt, orc, cuda, kind, dims, grid):
     """The two-factor kernel fused with the box-list transpose (default for
