@@ -1,7 +1,10 @@
-// Two-factor batched FFT for lengths m = M1 * M2 without a warp-aligned
-// schedule (odd 7-smooth lengths such as 105, 175, 225, 378): the four-step
-// decomposition inside one CTA, with both factor transforms held in one
-// thread's registers.  C2C rows and columns; rows of the real modes (R2C / C2R
+// Two-factor batched FFT for the 7-smooth lengths m = M1 * M2 (40 .. 1024)
+// that have no warp-per-row tile kernel (105, 175, 225, 378, 1000, ...): the
+// four-step decomposition inside one CTA, with both factor transforms held in
+// one thread's registers.  Three forms: fft2f_kernel (rows or columns, loads
+// straight from global memory), fft2f_pipe_kernel (contiguous rows streamed
+// through a bulk-copy ring) and fft2f_xpose_kernel (rows fused with the grid
+// transpose).  C2C rows and columns; rows of the real modes (R2C / C2R
 // through an m-point core: half length for even n, full length for odd n),
 // whose pre-processing is folded into phase A's loads and post-processing
 // into phase B's stores (R2C of even n pairs outputs k and m - k, so it
