@@ -770,28 +770,31 @@ def run_ours(args):
 
     # e2e: host buffers through the C ABI.  Every step copies its input from
     # pinned host memory, runs forward + backward, and copies the result back;
-    # consecutive steps are pipelined over two device buffer sets and three
+    # consecutive steps are pipelined over three device buffer sets and three
     # streams (host->device, compute on the plan's stream, device->host), so the
-    # copies of one step overlap the transforms of its neighbours.  The timed
-    # region spans the first copy-in to the last copy-out.
+    # copies of one step overlap the transforms of its neighbours and the other
+    # direction's copies.  The timed region spans the first copy-in to the last
+    # copy-out.
     e2e_ms = link_ms = None
     e2e_windows = []
+    link_windows = []
     if not args.no_e2e:
         host_in = torch.empty(n, dtype=torch.complex64, pin_memory=True)
         host_in.copy_(x0.cpu())
-        host_out = [torch.empty(n, dtype=torch.complex64, pin_memory=True) for _ in range(2)]
-        sets = [(a, b)] + [(torch.empty_like(a), torch.empty_like(a))]
+        NSETS = 3
+        host_out = [torch.empty(n, dtype=torch.complex64, pin_memory=True) for _ in range(NSETS)]
+        sets = [(a, b)] + [(torch.empty_like(a), torch.empty_like(a)) for _ in range(NSETS - 1)]
         s_in = torch.cuda.Stream(dev)
         s_out = torch.cuda.Stream(dev)
         e2e_steps = max(2, min(args.steps, 10))
-        ev = {k: [torch.cuda.Event() for _ in range(2)] for k in ("in", "comp", "out")}
+        ev = {k: [torch.cuda.Event() for _ in range(NSETS)] for k in ("in", "comp", "out")}
         for e in ev["out"]:
             e.record(s_out)
 
         def e2e_step(k):
-            i = k % 2
+            i = k % NSETS
             da, db = sets[i]
-            s_in.wait_event(ev["out"][i])            # the copy-out two steps back has read this set
+            s_in.wait_event(ev["out"][i])            # the copy-out NSETS steps back has read this set
             with torch.cuda.stream(s_in):
                 da.copy_(host_in, non_blocking=True)
             ev["in"][i].record(s_in)
@@ -804,7 +807,7 @@ def run_ours(args):
                 host_out[i].copy_(da, non_blocking=True)
             ev["out"][i].record(s_out)
 
-        for k in range(2):
+        for k in range(NSETS):
             e2e_step(k)
         torch.cuda.synchronize()
         # three windows of e2e_steps steps; the median window is reported (the
@@ -822,27 +825,31 @@ def run_ours(args):
             e2e_windows.append(f0.elapsed_time(f1) / e2e_steps)
         e2e_ms = sorted(e2e_windows)[1]
         # the round trip survived the pipeline: last result == input (scaled)
-        e2e_rt = float(torch.linalg.vector_norm(host_out[(e2e_steps - 1) % 2] / (DIMS[0] * DIMS[1] * DIMS[2])
+        e2e_rt = float(torch.linalg.vector_norm(host_out[(e2e_steps - 1) % NSETS] / (DIMS[0] * DIMS[1] * DIMS[2])
                                                 - host_in) / torch.linalg.vector_norm(host_in))
         # the host link alone: the same two copies per step, both directions
         # at once, no transforms - the bound the end-to-end figure runs into
-        ca, cb = sets[1]
-        lk0 = torch.cuda.Event(enable_timing=True)
-        lk1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        lk0.record(s_in)
-        s_out.wait_event(lk0)
-        for _ in range(e2e_steps):
-            with torch.cuda.stream(s_in):
-                ca.copy_(host_in, non_blocking=True)
-            with torch.cuda.stream(s_out):
-                host_out[0].copy_(cb, non_blocking=True)
-        lk_in = torch.cuda.Event()
-        lk_in.record(s_in)
-        s_out.wait_event(lk_in)
-        lk1.record(s_out)
-        torch.cuda.synchronize()
-        link_ms = lk0.elapsed_time(lk1) / e2e_steps
+        # (three windows, median, as for the end-to-end figure)
+        link_windows = []
+        for _ in range(3):
+            lk0 = torch.cuda.Event(enable_timing=True)
+            lk1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            lk0.record(s_in)
+            s_out.wait_event(lk0)
+            for k in range(e2e_steps):
+                ca, cb = sets[k % NSETS]
+                with torch.cuda.stream(s_in):
+                    ca.copy_(host_in, non_blocking=True)
+                with torch.cuda.stream(s_out):
+                    host_out[(k + 1) % NSETS].copy_(sets[(k + 1) % NSETS][1], non_blocking=True)
+            lk_in = torch.cuda.Event()
+            lk_in.record(s_in)
+            s_out.wait_event(lk_in)
+            lk1.record(s_out)
+            torch.cuda.synchronize()
+            link_windows.append(lk0.elapsed_time(lk1) / e2e_steps)
+        link_ms = sorted(link_windows)[1]
         e2e_ms, link_ms = max_over_ranks([e2e_ms, link_ms], world, dev)
         del sets
 
@@ -922,10 +929,11 @@ def run_ours(args):
             "kernels": [{"name": k, "launches": c, "total_ms": t} for k, c, t in sorted(prof, key=lambda r: -r[2])],
             "e2e": ({"value": world * 1000.0 / e2e_ms, "unit": "cycles/s", "h2d_bytes_per_step": nbytes,
                      "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms, "roundtrip_rel_l2": e2e_rt,
-                     "pipelined": "2 buffer sets; copy-in, compute, copy-out streams",
+                     "pipelined": "3 buffer sets; copy-in, compute, copy-out streams",
                      "windows_ms_per_step": e2e_windows, "reported": "median of 3 windows",
                      "host_link_bound": {"value": world * 1000.0 / link_ms, "unit": "cycles/s", "ms_per_step": link_ms,
-                                         "what": "the step's H2D and D2H copies alone, concurrently"}}
+                                         "what": "the step's H2D and D2H copies alone, concurrently",
+                                         "windows_ms_per_step": link_windows, "reported": "median of 3 windows"}}
                     if e2e_ms else None),
             "gpu_launches": launches,
             "autotune": _tune_records(dt) if args.effort == 3 else None,
