@@ -1226,9 +1226,9 @@ dtfft_error_t FftPlan::autotune(cudaStream_t s, int warmup, int iters, bool log)
 // ---------------------------------------------------------------------------
 // Tensor-store write-out of a fused tile pass (fft_tile_xpose_tma_kernel):
 // the pass's source groups and destination segments, its launch shape, and
-// the tensor maps of the last few output buffers (a map holds the buffer's
-// address, so it is encoded on the host the first time a buffer is seen; a
-// pure host computation, also legal while a stream is being captured).
+// the tensor maps of the last few (input, output) buffer pairs (a map holds the
+// buffer's address, so it is encoded on the host the first time a pair is
+// seen; a pure host computation, also legal while a stream is being captured).
 struct XTma {
     std::vector<FGroup> groups;
     std::vector<FSeg> segs;
@@ -1242,7 +1242,8 @@ struct XTma {
     size_t smem = 0;
     int box_i = 256;               // points per tensor store: 256, 128, 64 or 32
     std::mutex mu;
-    std::vector<std::pair<const void*, TmaXMaps*>> maps;   // per output pointer, most recent last
+    int m = 0;                     // points per row
+    std::vector<std::pair<std::pair<const void*, const void*>, TmaXMaps*>> maps;   // per (input, output), most recent last
     ~XTma() { for (auto& e : maps) delete e.second; }
 };
 
@@ -1267,8 +1268,12 @@ static bool xtma_fits(int m, int es, const std::vector<FSeg>& segs, int box_i = 
 
 // Tensor maps of every destination segment of the pass for output `out`:
 // (u in 8-byte words, i, w) of the segment's block, boxes of one line (u, 128
-// or 64 bytes) by up to 256 points, swizzled over the line's span.
-static dtfft_error_t xtma_encode(const XTma& x, int es, void* out, TmaXMaps* mp) {
+// or 64 bytes) by up to 256 points, swizzled over the line's span.  With
+// input `in` (non-null), also the load maps of the source groups whose rows
+// are not adjacent: (row words in runs of 256, run, u, w), one box = a tile of
+// S whole rows (one tensor load per tile instead of S row copies); `loads`
+// stays 0 when a group does not fit (every tile then takes bulk copies).
+static dtfft_error_t xtma_encode(const XTma& x, int es, const void* in, void* out, TmaXMaps* mp) {
     typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -1291,6 +1296,30 @@ static dtfft_error_t xtma_encode(const XTma& x, int es, void* out, TmaXMaps* mp)
                                x.lb == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                                CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return DTFFT_ERROR_GPU_CALL_FAILED;
+    }
+    const char* le = getenv("DTFFT_GB_XTMA_TILE_LOADS");   // measurements: 0 = bulk copies only
+    const i64 words = (i64)x.m * es / 8;
+    bool strided = false;
+    for (const FGroup& g : x.groups) strided = strided || g.su != x.m;
+    if (in && strided && !(le && le[0] == '0') && (int)x.groups.size() <= kTmaXMaxGroups && words % 256 == 0 &&
+        words / 256 <= 256) {
+        bool ok = true;
+        for (size_t gi = 0; gi < x.groups.size() && ok; ++gi) {
+            const FGroup& g = x.groups[gi];
+            if (g.su == x.m) continue;   // adjacent rows: one bulk copy per tile
+            cuuint64_t gdim[4] = {256, (cuuint64_t)(words / 256), (cuuint64_t)g.nu, (cuuint64_t)std::max(g.nw, 1)};
+            cuuint64_t gstr[3] = {256 * 8, (cuuint64_t)(g.su * es), (cuuint64_t)(std::max<i64>(g.sw, 1) * es)};
+            if (g.nw <= 1) gstr[2] = gstr[1] * (cuuint64_t)g.nu;
+            cuuint32_t box[4] = {256, (cuuint32_t)(words / 256), (cuuint32_t)x.S, 1};
+            cuuint32_t estr[4] = {1, 1, 1, 1};
+            const void* base = (const char*)in + g.src_off * es;
+            ok = ((uintptr_t)base % 16) == 0 && gstr[1] % 16 == 0 && gstr[2] % 16 == 0 && gstr[1] < (1ULL << 40) &&
+                 gstr[2] < (1ULL << 40) &&
+                 enc(&mp->lmap[gi], CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, const_cast<void*>(base), gdim, gstr, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+        }
+        mp->loads = ok ? 1 : 0;
     }
     return DTFFT_SUCCESS;
 }
@@ -1422,6 +1451,7 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
             tma_encode_tiled_fn() && xtma_fits(m, (int)es, segs, box)) {
             XTma* x = new XTma();
             x->box_i = box;
+            x->m = m;
             x->S = xs;
             x->lb = xs * (int)es;
             x->ncw = xw;
@@ -1444,7 +1474,7 @@ dtfft_error_t FusedFT::create(const BoxList& bl, int m, int dbl, bool tile_only,
             // the driver validates the maps' shapes and strides when they are
             // encoded: try once on an aligned stand-in address (host only)
             TmaXMaps probe;
-            const bool encodable = xtma_encode(*x, (int)es, (void*)(uintptr_t)4096, &probe) == DTFFT_SUCCESS;
+            const bool encodable = xtma_encode(*x, (int)es, nullptr, (void*)(uintptr_t)4096, &probe) == DTFFT_SUCCESS;
             bool ok = encodable && x->nst >= 2 && x->tiles <= 0x7fffffffLL &&
                       set_smem_attrs(fk, x->smem) == DTFFT_SUCCESS && set_smem_attrs(bk, x->smem) == DTFFT_SUCCESS;
             if (ok && xs != ts.S) {
@@ -1575,13 +1605,13 @@ static dtfft_error_t launch_fused_tile_tma(int m, XTma& x, const void* tw, const
         std::lock_guard<std::mutex> lk(x.mu);
         TmaXMaps* mp = nullptr;
         for (auto& e : x.maps)
-            if (e.first == out) mp = e.second;
+            if (e.first.first == in && e.first.second == out) mp = e.second;
         if (!mp) {
             mp = new TmaXMaps();
-            const dtfft_error_t r = xtma_encode(x, (int)sizeof(C), out, mp);
+            const dtfft_error_t r = xtma_encode(x, (int)sizeof(C), in, out, mp);
             if (r != DTFFT_SUCCESS) { delete mp; return r; }
             if (x.maps.size() >= 4) { delete x.maps.front().second; x.maps.erase(x.maps.begin()); }
-            x.maps.emplace_back(out, mp);
+            x.maps.emplace_back(std::make_pair(in, (const void*)out), mp);
         }
         memcpy(&X.m, mp, sizeof(TmaXMaps));
     }

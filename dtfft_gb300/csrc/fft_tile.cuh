@@ -521,8 +521,14 @@ __global__ void __launch_bounds__(32 * (NCW + NSW), 1) fft_tile_xpose_kernel(TAr
 constexpr int kTmaXMaxSegs = 48;
 constexpr int kTileHdrXTma = 1024;   // header; the launch adds another 1 KB of alignment slack
 
+constexpr int kTmaXMaxGroups = 16;
 struct TmaXMaps {
     CUtensorMap map[kTmaXMaxSegs];   // per destination segment: (u words, i, w) of its block
+    // per source group whose rows are not adjacent: (row words in 256-word
+    // runs, run, u, w), one box = a whole tile of S rows; unused when `loads`
+    // is 0 (every tile is then one contiguous bulk copy or per-row copies)
+    CUtensorMap lmap[kTmaXMaxGroups];
+    int loads;
 };
 
 template <typename R>
@@ -543,6 +549,13 @@ __device__ __forceinline__ bool bar_red_or(int id, int nthreads, bool v) {
 }
 __device__ __forceinline__ void bar_sync_n(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(const CUtensorMap* map, void* smem, int c2, int c3, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(smem)),
+        "l"(map), "r"(0), "r"(0), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
 }
 __device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* smem, int c0, int c1, int c2) {
     asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(map),
@@ -653,8 +666,21 @@ __global__ void __launch_bounds__(32 * (NCW + 1), 1) fft_tile_xpose_tma_kernel(c
 
     // ---- producer warp: bulk loads in, tensor stores out ----
     if (lane != 0) return;
+    // strided source rows: one tensor load of the whole tile (its box always
+    // fills S rows; rows past the block's end read as zeros), else bulk copies
     auto issue = [&](i64 tj, int bj) {
-        tile_issue<R, true, M>(A, tj, reinterpret_cast<C*>(ring + (size_t)bj * M * LB), &full[bj]);
+        C* buf = reinterpret_cast<C*>(ring + (size_t)bj * M * LB);
+        if (X.m.loads) {
+            i64 row0, rs;
+            int nrows, gi, u0, w;
+            tile_geom<R, true, M>(A, tj, row0, rs, nrows, gi, u0, w);
+            if (rs != M) {
+                mbar_expect_tx(&full[bj], (uint32_t)(M * sizeof(C)) * (uint32_t)S);
+                tma_load_4d(&X.m.lmap[gi], buf, u0, w, &full[bj]);
+                return;
+            }
+        }
+        tile_issue<R, true, M>(A, tj, buf, &full[bj]);
     };
     uint32_t issued_par = 0;   // bit b: parity of the last load into buffer b
     for (int j = 0; j < NST; ++j) {
