@@ -217,9 +217,10 @@ def _tune_records(dt):
         k = r["chosen"].split(":")[0]
         kinds[k] = kinds.get(k, 0) + 1
     gain = sorted(recs, key=lambda r: -(r["runner_up_ms"] - r["chosen_ms"]) if r["runner_up"] else 0)
+    fused = [r for r in gain if r["step"].startswith("fused")]
     return {"steps_tuned": len(recs), "candidates_timed": sum(r["candidates"] for r in recs),
             "chosen_kinds": kinds, "largest_margins": gain[:12],
-            "fused_passes": [r for r in recs if r["step"].startswith("fused")]}
+            "fused_passes_tuned": len(fused), "fused_passes": fused[:12]}
 
 
 def batched_section(args, dt, dev, stream, peak):
