@@ -412,7 +412,9 @@ def tensor_core_section(args, dt, dev, stream, sizes=(768, 1024)):
     """C2C complex64 N^3 (one process, Z-slab plan), inputs uniform[-1,1) re/im
     plus 1e3-amplitude spikes at 0.1% of the points: FP32 Stockham row passes
     against the tensor-core form (DFT-matrix GEMMs on tcgen05, FP16 hi + lo,
-    FP32 accumulate), fwd+bwd cycles/s, forward error against an FP64
+    FP32 accumulate) of the plain row passes (both plans keep the fused FFT +
+    transpose passes on the FP32 kernels; `row_pass_ms` compares the two row
+    kernels alone), fwd+bwd cycles/s, forward error against an FP64
     (complex128) plan of the same transform, and against numpy FP64 values of
     five Z-lines of the spectrum."""
     import torch

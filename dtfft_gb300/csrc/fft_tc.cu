@@ -14,14 +14,18 @@
 // and the lo parts stay normal numbers.
 //
 // One CTA of 128 threads owns S = 128 / R1 rows per tile and walks tiles
-// persistently.  Thread t builds A row t of stage 1 and, after the MMA, reads
+// persistently; two to four such CTAs share an SM.  Thread t builds A row t of stage 1 and, after the MMA, reads
 // TMEM lane t back (tcgen05.ld), applies the twiddles and scatters stage 2's
 // A rows; one elected thread issues the tcgen05.mma instructions and commits
-// them to an mbarrier.  Every wait is bounded: on timeout the kernel records
-// an error code in the status word, waits (bounded) once more for its own MMAs
-// and frees its tensor memory before returning.
+// them to an mbarrier.  The loads of the next tile's input are issued as soon
+// as this tile's stage-1 operand is in shared memory, so they are in flight
+// while this tile multiplies and writes; each thread keeps its R2 stage-1
+// twiddles in registers for all tiles.  Every wait is bounded: on timeout the
+// kernel records an error code in the status word, waits (bounded) once more
+// for its own MMAs and frees its tensor memory before returning.
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -103,6 +107,20 @@ __device__ __forceinline__ float pow2_scale(float amax, int& e) {
     return __uint_as_float((uint32_t)(127 + 14 - e) << 23);
 }
 
+// Stage-2 A operand: thread (s1, n1) writes 4 bytes (one complex value) at
+// K = 2 n1 of row s1 R2 + k2, so a warp's 32 lanes write one row (R1 = 32) or
+// two rows R2 apart (R1 = 16).  With core matrices adjacent in K 128 bytes
+// apart those writes fall on 4 banks (8-way conflicts); 144 bytes apart they
+// fall on 32 (R1 = 32) or 16 banks per row, and the distance between the 8-row
+// groups is padded so that a warp's two rows sit 16 banks apart.
+constexpr int kTcLbo2 = 144;
+constexpr int tc_sbo2(int R1, int R2) {
+    int s = (2 * R1 / 8) * kTcLbo2;
+    if (R1 == 16)
+        while ((((R2 / 8) * s / 4) & 31) != 16) s += 16;
+    return s;
+}
+
 template <int R1, int R2>
 struct TcShape {
     static constexpr int M = R1 * R2;
@@ -111,7 +129,8 @@ struct TcShape {
     static constexpr int K2 = 2 * R1, N2 = 2 * R1;     // stage 2 GEMM (real)
     static constexpr int G2 = (S * R2 + 127) / 128;    // stage-2 groups of 128 vectors
     static constexpr int B1 = N1 * K1 * 2, B2 = N2 * K2 * 2;   // bytes of one fp16 B operand
-    static constexpr int A1 = 128 * K1 * 2, A2 = G2 * 128 * K2 * 2;
+    static constexpr int LBO2 = kTcLbo2, SBO2 = tc_sbo2(R1, R2);
+    static constexpr int A1 = 128 * K1 * 2, A2 = G2 * 16 * SBO2;
     static constexpr int OFF_B1H = 0, OFF_B1L = B1, OFF_B2H = 2 * B1, OFF_B2L = 2 * B1 + B2;
     static constexpr int OFF_A1H = 2 * (B1 + B2), OFF_A1L = OFF_A1H + A1;
     static constexpr int OFF_A2H = OFF_A1L + A1, OFF_A2L = OFF_A2H + A2;
@@ -125,7 +144,28 @@ struct TcShape {
     static_assert(N1 % 16 == 0 && N2 % 16 == 0 && N1 <= 256 && N2 <= 256, "N for M = 128");
     static_assert(N1 % 16 == 0 && N2 % 16 == 0, "TMEM loads of 16 columns");
     static_assert(COLS_USED <= 256, "tensor memory budget");
+    static_assert(R1 == 16 || R1 == 32, "one or two stage-2 rows per warp");
+    static_assert(SBO2 % 16 == 0 && SBO2 >= (K2 / 8) * LBO2, "stage-2 core matrices do not overlap");
 };
+
+// byte offset of element (row, k) of the padded stage-2 A operand (row < 128 * G2)
+template <int R1, int R2>
+__device__ __forceinline__ uint32_t a2_off(int row, int k) {
+    typedef TcShape<R1, R2> SH;
+    return (uint32_t)((row >> 7) * (16 * SH::SBO2) + ((row & 127) >> 3) * SH::SBO2 + (k >> 3) * SH::LBO2 +
+                      (row & 7) * 16 + (k & 7) * 2);
+}
+
+// stage-1 input of this thread (row s1 of the tile, points n1 + R1 n2);
+// zeros past the last row
+template <int R1, int R2>
+__device__ __forceinline__ void tc_load_input(const TcArgs& A, i64 tile, int s1, int n1, float2 (&x)[R2]) {
+    const i64 sig = tile * (128 / R1) + s1;
+    const bool live = sig < A.nsig;
+    const float2* src = A.in + (live ? sig : 0) * (i64)(R1 * R2) + n1;
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2) x[n2] = live ? src[R1 * n2] : make_float2(0.f, 0.f);
+}
 
 template <int R1, int R2>
 __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
@@ -166,19 +206,18 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
     bool failed = false;
 
     const int s1 = t / R1, n1 = t % R1;     // stage-1 row of this thread
+    float2 tw[R2];                          // W_m^(n1 k2), the same on every tile
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) tw[k2] = __ldg(&A.tw[(n1 * k2) % SH::M]);
+    float2 x[R2];
+    tc_load_input<R1, R2>(A, (i64)blockIdx.x, s1, n1, x);
     for (i64 tile = blockIdx.x; tile < A.ntiles && !failed; tile += gridDim.x) {
         const i64 sig0 = tile * SH::S;
         // ---- stage 1 operand: row t = (s1, n1), k = 2*n2 + {re, im} ----
         {
-            const i64 sig = sig0 + s1;
-            const bool live = sig < A.nsig;
-            float2 x[R2];
             float amax = 0.f;
 #pragma unroll
-            for (int n2 = 0; n2 < R2; ++n2) {
-                x[n2] = live ? A.in[sig * SH::M + n1 + R1 * n2] : make_float2(0.f, 0.f);
-                amax = fmaxf(amax, fmaxf(fabsf(x[n2].x), fabsf(x[n2].y)));
-            }
+            for (int n2 = 0; n2 < R2; ++n2) amax = fmaxf(amax, fmaxf(fabsf(x[n2].x), fabsf(x[n2].y)));
 #pragma unroll
             for (int o = 1; o < R1; o <<= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
             int e;
@@ -220,6 +259,9 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
             }
             tc_commit(bar);
         }
+        // x is in the stage-1 operand: load the next tile's input now, so its
+        // loads are in flight while this tile multiplies and writes
+        tc_load_input<R1, R2>(A, tile + gridDim.x, s1, n1, x);
         // every thread leaves together when a wait times out
         if (__syncthreads_or(!mbar_wait_bounded(bar, phase))) { failed = true; break; }
         phase ^= 1;
@@ -236,13 +278,12 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
                 for (int j = 0; j < 8; ++j) {
                     const int k2 = c0 / 2 + j;
                     float2 y = make_float2(acc[2 * j], acc[2 * j + 1]);
-                    const float2 w = __ldg(&A.tw[(n1 * k2) % SH::M]);
+                    const float2 w = tw[k2];
                     const float2 z = make_float2((y.x * w.x - y.y * w.y) * sc2, (y.x * w.y + y.y * w.x) * sc2);
                     const __half hr = __float2half_rn(z.x), hi_ = __float2half_rn(z.y);
                     const __half lr = __float2half_rn(z.x - __half2float(hr));
                     const __half li = __float2half_rn(z.y - __half2float(hi_));
-                    const int r2 = s1 * R2 + k2;
-                    const uint32_t off = (uint32_t)((r2 >> 7) * (128 * SH::K2 * 2)) + kmaj_off(r2 & 127, 2 * n1, SH::K2);
+                    const uint32_t off = a2_off<R1, R2>(s1 * R2 + k2, 2 * n1);
                     *reinterpret_cast<__half2*>(sm + SH::OFF_A2H + off) = __halves2half2(hr, hi_);
                     *reinterpret_cast<__half2*>(sm + SH::OFF_A2L + off) = __halves2half2(lr, li);
                 }
@@ -256,14 +297,14 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
 #pragma unroll
             for (int g = 0; g < SH::G2; ++g) {
                 const uint32_t dcol = tmem + (uint32_t)(SH::N1 + g * SH::N2);
-                const uint32_t ag = (uint32_t)(g * 128 * SH::K2 * 2);
+                const uint32_t ag = (uint32_t)(g * 16 * SH::SBO2);
 #pragma unroll
                 for (int j = 0; j < SH::K2 / 16; ++j) {
-                    const uint32_t ka = 256u * j;
-                    const uint64_t ah = smem_desc(sbase + SH::OFF_A2H + ag + ka, 128, SH::K2 * 16);
-                    const uint64_t al = smem_desc(sbase + SH::OFF_A2L + ag + ka, 128, SH::K2 * 16);
-                    const uint64_t bh = smem_desc(sbase + SH::OFF_B2H + ka, 128, SH::K2 * 16);
-                    const uint64_t bl = smem_desc(sbase + SH::OFF_B2L + ka, 128, SH::K2 * 16);
+                    const uint32_t ka = 2u * SH::LBO2 * j, kb = 256u * j;
+                    const uint64_t ah = smem_desc(sbase + SH::OFF_A2H + ag + ka, SH::LBO2, SH::SBO2);
+                    const uint64_t al = smem_desc(sbase + SH::OFF_A2L + ag + ka, SH::LBO2, SH::SBO2);
+                    const uint64_t bh = smem_desc(sbase + SH::OFF_B2H + kb, 128, SH::K2 * 16);
+                    const uint64_t bl = smem_desc(sbase + SH::OFF_B2L + kb, 128, SH::K2 * 16);
                     tc_mma(dcol, ah, bh, id2, j > 0 ? 1u : 0u);
                     tc_mma(dcol, ah, bl, id2, 1u);
                     tc_mma(dcol, al, bh, id2, 1u);
@@ -317,11 +358,11 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
 // host side
 // ---------------------------------------------------------------------------
 
-struct TcKernel { int R1, R2; const void* fn; int smem; };
+struct TcKernel { int R1, R2; const void* fn; int smem; int tmem_cols; };
 
 template <int R1, int R2>
 static TcKernel tc_entry() {
-    return TcKernel{R1, R2, (const void*)fft_tc_kernel<R1, R2>, TcShape<R1, R2>::SMEM};
+    return TcKernel{R1, R2, (const void*)fft_tc_kernel<R1, R2>, TcShape<R1, R2>::SMEM, TcShape<R1, R2>::TMEM_COLS};
 }
 
 // row lengths with a tensor-core form: m = R1 * R2
@@ -403,12 +444,26 @@ dtfft_error_t tc_create(int m, void** out) {
             e = DTFFT_ERROR_GPU_CALL_FAILED;
     }
     if (e == DTFFT_SUCCESS) {
+        // CTAs per SM: as many as the kernel's registers and shared memory
+        // (largest carveout) leave room for, at most 4 and within the SM's 512
+        // tensor-memory columns, so no CTA waits in tcgen05.alloc.  The
+        // occupancy query answers 1 for this kernel, so the count is made here.
+        // Measured on 1 GiB batches: 2 CTAs per SM take 256/512/768/1024-point
+        // rows from 617/525/590/568 us to 461/495/525/502 us, 4 (256 points
+        // only; the others fit 2) to 430 us.  DTFFT_GB_TC_CTAS=k lowers or
+        // raises the limit of 4 (experiments).
+        int cap = 4;
+        if (const char* ce = getenv("DTFFT_GB_TC_CTAS"))
+            if (atoi(ce) > 0) cap = atoi(ce);
+        cudaFuncAttributes fa;
         if (cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, k.smem) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f->per_sm, k.fn, 128, k.smem) != cudaSuccess ||
-            f->per_sm < 1)
+            cudaFuncSetAttribute(k.fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess ||
+            cudaFuncGetAttributes(&fa, k.fn) != cudaSuccess)
             e = DTFFT_ERROR_GPU_CALL_FAILED;
-        // each CTA holds up to 256 tensor-memory columns of the SM's 512
-        f->per_sm = std::min(f->per_sm, 2);
+        else
+            f->per_sm = std::min({65536 / (std::max(fa.numRegs, 1) * 128), (227 * 1024) / (k.smem + 1024), cap,
+                                  512 / k.tmem_cols});
+        f->per_sm = std::max(f->per_sm, 1);
         int dev = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&f->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || f->sms < 1)

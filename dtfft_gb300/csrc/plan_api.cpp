@@ -226,9 +226,12 @@ static dtfft_error_t build_fused(Plan& p) {
     // two-factor kernel takes the rows (they beat FFT + transpose there).
     // DTFFT_GB_FUSE=1 also fuses the other lengths with the register kernels;
     // DTFFT_GB_FUSE=0 keeps every step unfused.
-    // The tensor-core form (fft_form() == 1) keeps its row passes unfused.
+    // Under the tensor-core form (fft_form() == 1) the fused passes stay on
+    // the FP32 tile / two-factor kernels and the plain row passes left over
+    // (a Z-slab plan's forward Z rows and backward X rows) run on tensor
+    // cores where their length has a tensor-core kernel.
     const char* fz = getenv("DTFFT_GB_FUSE");
-    if ((fz && strcmp(fz, "0") == 0) || fft_form() == 1) return DTFFT_SUCCESS;
+    if (fz && strcmp(fz, "0") == 0) return DTFFT_SUCCESS;
     const bool tile_only = !(fz && strcmp(fz, "1") == 0);
     const int dbl = p.precision == DTFFT_DOUBLE ? 1 : 0;
     std::vector<std::pair<int, int>> steps;   // (transpose type, FFT dim on its send layout)

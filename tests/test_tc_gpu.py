@@ -43,7 +43,11 @@ def _kernel_names(L):
     return names
 
 
-@pytest.mark.parametrize("n,howmany", [(256, 1000), (512, 333), (768, 130), (1024, 67), (512, 3)])
+# (256, 7301) and (1024, 3651): about three tiles per CTA of the 304-CTA grid
+# with a ragged last tile (each CTA loads its next tile while the current one
+# multiplies)
+@pytest.mark.parametrize("n,howmany", [(256, 1000), (512, 333), (768, 130), (1024, 67), (512, 3),
+                                       (256, 7301), (1024, 3651)])
 def test_tc_rows_match_fp64(dt, cuda, tc_form, n, howmany):
     import torch
     L = tc_form
@@ -75,9 +79,15 @@ def test_tc_rows_match_fp64(dt, cuda, tc_form, n, howmany):
     assert L.gb_fft_destroy(ctypes.byref(h)) == 0
 
 
-@pytest.mark.parametrize("dims", [[512, 40, 48], [768, 36, 32], [1024, 24, 20]])
+# The fused FFT + transpose passes stay on the FP32 kernels; the plain row
+# passes left over (the forward Z rows of these one-process Z-slab plans) run
+# on tensor cores where Z has a tensor-core length.
+@pytest.mark.parametrize("dims", [[512, 40, 48], [768, 36, 32], [1024, 24, 20],
+                                  [40, 48, 512], [36, 32, 768], [24, 20, 1024]])
 def test_tc_plan_forward_matches_fp64(dt, cuda, tc_form, dims):
     import torch
+    L = tc_form
+    L.dtfft_gb_profile_count.restype = ctypes.c_int32
     plan = dt.PlanC2C(dims, precision=dt.Precision.SINGLE, executor=dt.Executor.CUFFT)
     n = plan.alloc_size
     g = _signal(tuple(dims[::-1]), seed=sum(dims))
@@ -85,8 +95,13 @@ def test_tc_plan_forward_matches_fp64(dt, cuda, tc_form, dims):
     a[: g.size] = torch.from_numpy(g.ravel()).to(cuda)
     b = torch.zeros_like(a)
     torch.cuda.synchronize()
+    L.dtfft_gb_profile_start()
     plan.execute(a, b, dt.Execute.FORWARD)
     torch.cuda.synchronize()
+    L.dtfft_gb_profile_stop()
+    if dims[2] in (256, 512, 768, 1024):
+        assert any(nm.startswith("ffttc_rows_c2c_m%d" % dims[2]) for nm in _kernel_names(L))
+    assert L.dtfft_gb_device_status(1) == 0
     ref = np.fft.fftn(g.astype(np.complex128))
     # Z pencils of a one-process plan: (Z, X, Y) with Z fastest
     ref = ref.transpose(1, 2, 0).ravel()

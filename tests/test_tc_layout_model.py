@@ -1,0 +1,117 @@
+"""CPU model of the tensor-core row kernel (dtfft_gb300/csrc/fft_tc.cu,
+fft_tc_kernel / TcShape): the two DFT-matrix GEMM stages with the kernel's
+operand indices give the DFT of each row, the stage-2 A operand's padded
+core-matrix strides place every (row, K) element once inside its buffer, the
+32 lanes of a warp write that operand without shared-memory bank conflicts,
+and the kernel's shared memory admits two CTAs per SM."""
+import numpy as np
+import pytest
+
+# (R1, R2) of the compiled kernels: m = R1 * R2 (tc_pick)
+SHAPES = [(16, 16), (16, 32), (32, 24), (32, 32)]
+LBO2 = 144
+
+
+def sbo2(R1, R2):
+    s = (2 * R1 // 8) * LBO2
+    if R1 == 16:
+        while ((R2 // 8) * s // 4) % 32 != 16:
+            s += 16
+    return s
+
+
+def shape(R1, R2):
+    S = 128 // R1
+    K1 = N1 = 2 * R2
+    K2 = N2 = 2 * R1
+    G2 = (S * R2 + 127) // 128
+    B1, B2 = N1 * K1 * 2, N2 * K2 * 2
+    A1 = 128 * K1 * 2
+    SB = sbo2(R1, R2)
+    A2 = G2 * 16 * SB
+    off_scale = 2 * (B1 + B2) + 2 * A1 + 2 * A2
+    smem = ((off_scale + 4 * S + 15) & ~15) + 16
+    return dict(S=S, K1=K1, K2=K2, N1=N1, N2=N2, G2=G2, SB=SB, A2=A2, smem=smem)
+
+
+def a2_off(r2, k, SB):
+    row = r2 & 127
+    return (r2 >> 7) * 16 * SB + (row >> 3) * SB + (k >> 3) * LBO2 + (row & 7) * 16 + (k & 7) * 2
+
+
+@pytest.mark.parametrize("R1,R2", SHAPES)
+def test_stage2_operand_layout(R1, R2):
+    sh = shape(R1, R2)
+    seen = set()
+    for r2 in range(sh["G2"] * 128):
+        for k in range(0, sh["K2"], 2):
+            a = a2_off(r2, k, sh["SB"])
+            assert a % 4 == 0 and 0 <= a and a + 4 <= sh["A2"]
+            assert a not in seen
+            seen.add(a)
+    # descriptor fields are 16-byte units; a core matrix (8 rows x 16 bytes) is contiguous
+    assert LBO2 % 16 == 0 and sh["SB"] % 16 == 0 and LBO2 >= 128
+    assert sh["SB"] >= (sh["K2"] // 8) * LBO2
+
+
+@pytest.mark.parametrize("R1,R2", SHAPES)
+def test_stage2_writes_conflict_free(R1, R2):
+    sh = shape(R1, R2)
+    for w in range(4):
+        for k2 in range(R2):
+            banks = {}
+            for lane in range(32):
+                t = 32 * w + lane
+                s1, n1 = t // R1, t % R1
+                a = a2_off(s1 * R2 + k2, 2 * n1, sh["SB"]) // 4
+                banks.setdefault(a % 32, set()).add(a)
+            assert max(len(v) for v in banks.values()) == 1
+
+
+@pytest.mark.parametrize("R1,R2", SHAPES)
+def test_two_ctas_per_sm(R1, R2):
+    assert 2 * (shape(R1, R2)["smem"] + 1024) <= 228 * 1024
+
+
+def real_dft(R, sign):
+    """Real 2R x 2R form of W_R^(j q): row 2j + a (output re/im), column 2q + b."""
+    Bm = np.zeros((2 * R, 2 * R))
+    for j in range(R):
+        for q in range(R):
+            ang = sign * 2 * np.pi * ((j * q) % R) / R
+            c, s = np.cos(ang), np.sin(ang)
+            Bm[2 * j:2 * j + 2, 2 * q:2 * q + 2] = [[c, -s], [s, c]]
+    return Bm
+
+
+@pytest.mark.parametrize("R1,R2", SHAPES)
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_two_stage_gemm_matches_dft(R1, R2, sign):
+    m = R1 * R2
+    sh = shape(R1, R2)
+    S = sh["S"]
+    rng = np.random.default_rng(m)
+    x = rng.standard_normal((S, m)) + 1j * rng.standard_normal((S, m))
+    tw = np.exp(sign * 2j * np.pi * np.arange(m) / m)
+    # stage 1: A row t = (s1, n1), k = 2 n2 + {re, im}
+    A1 = np.zeros((128, 2 * R2))
+    for t in range(128):
+        s1, n1 = t // R1, t % R1
+        v = x[s1, n1 + R1 * np.arange(R2)]
+        A1[t, 0::2], A1[t, 1::2] = v.real, v.imag
+    D1 = A1 @ real_dft(R2, sign).T          # D[v][n] = sum_k A[v][k] B[n][k]
+    # twiddles and stage-2 rows r2 = (s1, k2), k = 2 n1 + {re, im}
+    A2 = np.zeros((sh["G2"] * 128, 2 * R1))
+    for t in range(128):
+        s1, n1 = t // R1, t % R1
+        y = D1[t, 0::2] + 1j * D1[t, 1::2]
+        z = y * tw[(n1 * np.arange(R2)) % m]
+        r2 = s1 * R2 + np.arange(R2)
+        A2[r2, 2 * n1], A2[r2, 2 * n1 + 1] = z.real, z.imag
+    D2 = A2 @ real_dft(R1, sign).T
+    out = np.zeros((S, m), dtype=complex)
+    for r2 in range(S * R2):
+        s, k2 = r2 // R2, r2 % R2
+        out[s, np.arange(R1) * R2 + k2] = D2[r2, 0::2] + 1j * D2[r2, 1::2]
+    ref = np.fft.fft(x, axis=1) if sign < 0 else np.fft.ifft(x, axis=1) * m
+    assert np.abs(out - ref).max() <= 1e-9 * np.abs(ref).max()
