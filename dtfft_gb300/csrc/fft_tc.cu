@@ -14,9 +14,9 @@
 // and the lo parts stay normal numbers.
 //
 // One CTA of 128 threads owns S = 128 / R1 rows per tile and walks tiles
-// persistently; two to four such CTAs share an SM.  Thread t builds A row t of stage 1 and, after the MMA, reads
-// TMEM lane t back (tcgen05.ld), applies the twiddles and scatters stage 2's
-// A rows; one elected thread issues the tcgen05.mma instructions and commits
+// persistently; three to five such CTAs share an SM.  Thread t builds A row t
+// of stage 1 and, after the MMA, reads TMEM lane t back (tcgen05.ld), applies
+// the twiddles and scatters stage 2's A rows; one elected thread issues the tcgen05.mma instructions and commits
 // them to an mbarrier.  The loads of the next tile's input are issued as soon
 // as this tile's stage-1 operand is in shared memory, so they are in flight
 // while this tile multiplies and writes; each thread keeps its R2 stage-1
@@ -132,9 +132,16 @@ struct TcShape {
     static constexpr int LBO2 = kTcLbo2, SBO2 = tc_sbo2(R1, R2);
     static constexpr int A1 = 128 * K1 * 2, A2 = G2 * 16 * SBO2;
     static constexpr int OFF_B1H = 0, OFF_B1L = B1, OFF_B2H = 2 * B1, OFF_B2L = 2 * B1 + B2;
+    // The stage-1 and stage-2 A operands share one region: a tile's stage-1
+    // MMAs have completed before its stage-2 operand is written, and its
+    // stage-2 MMAs before the next tile's stage-1 operand is.  Rows of the
+    // stage-2 operand past the tile's S * R2 vectors (768 points) then hold
+    // stage-1 values; each output row of an MMA depends on its own A row only,
+    // and those rows' results are never stored.
     static constexpr int OFF_A1H = 2 * (B1 + B2), OFF_A1L = OFF_A1H + A1;
-    static constexpr int OFF_A2H = OFF_A1L + A1, OFF_A2L = OFF_A2H + A2;
-    static constexpr int OFF_SCALE = OFF_A2L + A2;                 // S floats
+    static constexpr int OFF_A2H = OFF_A1H, OFF_A2L = OFF_A2H + A2;
+    static constexpr int A_REGION = 2 * (A1 > A2 ? A1 : A2);
+    static constexpr int OFF_SCALE = OFF_A1H + A_REGION;           // S floats
     static constexpr int OFF_BAR = (OFF_SCALE + 4 * S + 15) & ~15;  // mbarrier + tmem slot
     static constexpr int SMEM = OFF_BAR + 16;
     static constexpr int COLS_USED = N1 + G2 * N2;
@@ -176,14 +183,14 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + SH::OFF_BAR + 8);
     float* scale_inv = reinterpret_cast<float*>(sm + SH::OFF_SCALE);
 
-    // B operands (hi/lo of both stages) and zeroed stage-2 A (its padding rows stay zero)
+    // B operands (hi/lo of both stages); the A region starts zeroed
     {
         const int nb = (2 * (SH::B1 + SH::B2)) / 16;
         uint4* dst = reinterpret_cast<uint4*>(sm);
         for (int i = t; i < nb; i += 128) dst[i] = A.bmat[i];
         uint4 z = make_uint4(0, 0, 0, 0);
-        uint4* a2 = reinterpret_cast<uint4*>(sm + SH::OFF_A2H);
-        for (int i = t; i < (2 * SH::A2) / 16; i += 128) a2[i] = z;
+        uint4* a = reinterpret_cast<uint4*>(sm + SH::OFF_A1H);
+        for (int i = t; i < SH::A_REGION / 16; i += 128) a[i] = z;
     }
     if (t == 0) {
         mbar_init(bar, 1);
@@ -445,14 +452,15 @@ dtfft_error_t tc_create(int m, void** out) {
     }
     if (e == DTFFT_SUCCESS) {
         // CTAs per SM: as many as the kernel's registers and shared memory
-        // (largest carveout) leave room for, at most 4 and within the SM's 512
-        // tensor-memory columns, so no CTA waits in tcgen05.alloc.  The
-        // occupancy query answers 1 for this kernel, so the count is made here.
-        // Measured on 1 GiB batches: 2 CTAs per SM take 256/512/768/1024-point
-        // rows from 617/525/590/568 us to 461/495/525/502 us, 4 (256 points
-        // only; the others fit 2) to 430 us.  DTFFT_GB_TC_CTAS=k lowers or
-        // raises the limit of 4 (experiments).
-        int cap = 4;
+        // (largest carveout) leave room for, within the SM's 512 tensor-memory
+        // columns so no CTA waits in tcgen05.alloc: 5 at 256 points (registers),
+        // 3 at 512 / 768 / 1024 (registers and shared memory).  The occupancy
+        // query answers 1 for this kernel, so the count is made here.
+        // Measured on 1 GiB batches of 256/512/768/1024-point rows: one CTA
+        // per SM 617/525/590/568 us, two 461/495/525/502 us, 5/3/3/3
+        // 409/438/457/437 us.  DTFFT_GB_TC_CTAS=k sets a lower limit
+        // (experiments).
+        int cap = 8;
         if (const char* ce = getenv("DTFFT_GB_TC_CTAS"))
             if (atoi(ce) > 0) cap = atoi(ce);
         cudaFuncAttributes fa;

@@ -3,7 +3,8 @@ fft_tc_kernel / TcShape): the two DFT-matrix GEMM stages with the kernel's
 operand indices give the DFT of each row, the stage-2 A operand's padded
 core-matrix strides place every (row, K) element once inside its buffer, the
 32 lanes of a warp write that operand without shared-memory bank conflicts,
-and the kernel's shared memory admits two CTAs per SM."""
+and the kernel's shared memory and tensor memory admit three or four CTAs
+per SM."""
 import numpy as np
 import pytest
 
@@ -29,9 +30,14 @@ def shape(R1, R2):
     A1 = 128 * K1 * 2
     SB = sbo2(R1, R2)
     A2 = G2 * 16 * SB
-    off_scale = 2 * (B1 + B2) + 2 * A1 + 2 * A2
+    # the stage-1 and stage-2 A operands (hi + lo each) share one region
+    a_region = 2 * max(A1, A2)
+    off_scale = 2 * (B1 + B2) + a_region
     smem = ((off_scale + 4 * S + 15) & ~15) + 16
-    return dict(S=S, K1=K1, K2=K2, N1=N1, N2=N2, G2=G2, SB=SB, A2=A2, smem=smem)
+    cols = N1 + G2 * N2
+    tmem = next(c for c in (32, 64, 128, 256) if cols <= c)
+    return dict(S=S, K1=K1, K2=K2, N1=N1, N2=N2, G2=G2, SB=SB, A1=A1, A2=A2, a_region=a_region,
+                smem=smem, tmem=tmem)
 
 
 def a2_off(r2, k, SB):
@@ -69,8 +75,14 @@ def test_stage2_writes_conflict_free(R1, R2):
 
 
 @pytest.mark.parametrize("R1,R2", SHAPES)
-def test_two_ctas_per_sm(R1, R2):
-    assert 2 * (shape(R1, R2)["smem"] + 1024) <= 228 * 1024
+def test_ctas_per_sm(R1, R2):
+    """Shared memory (227 KB per CTA budget, 1 KB reserved each) and the SM's
+    512 tensor-memory columns admit three CTAs per SM, four at 256 points."""
+    sh = shape(R1, R2)
+    want = 4 if R1 * R2 == 256 else 3
+    assert (227 * 1024) // (sh["smem"] + 1024) >= want
+    assert 512 // sh["tmem"] >= want
+    assert 2 * sh["A1"] <= sh["a_region"] and 2 * sh["A2"] <= sh["a_region"]
 
 
 def real_dft(R, sign):
