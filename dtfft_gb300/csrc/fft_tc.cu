@@ -16,8 +16,9 @@
 // One CTA of 128 threads owns S = 128 / R1 rows per tile and walks tiles
 // persistently; three to five such CTAs share an SM.  Thread t builds A row t
 // of stage 1 and, after the MMA, reads TMEM lane t back (tcgen05.ld), applies
-// the twiddles and scatters stage 2's A rows; one elected thread issues the tcgen05.mma instructions and commits
-// them to an mbarrier.  The loads of the next tile's input are issued as soon
+// the twiddles and scatters stage 2's A rows; one elected thread issues the
+// tcgen05.mma instructions and commits them to an mbarrier.  The loads of the
+// next tile's input are issued as soon
 // as this tile's stage-1 operand is in shared memory, so they are in flight
 // while this tile multiplies and writes; each thread keeps its R2 stage-1
 // twiddles in registers for all tiles.  Every wait is bounded: on timeout the
