@@ -18,10 +18,11 @@
 // of stage 1 and, after the MMA, reads TMEM lane t back (tcgen05.ld), applies
 // the twiddles and scatters stage 2's A rows; one elected thread issues the
 // tcgen05.mma instructions and commits them to an mbarrier.  The loads of the
-// next tile's input are issued as soon
-// as this tile's stage-1 operand is in shared memory, so they are in flight
-// while this tile multiplies and writes; each thread keeps its R2 stage-1
-// twiddles in registers for all tiles.  Every wait is bounded: on timeout the
+// next tile's input are issued as soon as this tile's stage-1 operand is in
+// shared memory, so they are in flight while this tile multiplies and writes;
+// the next tile's stage-1 MMAs run while this tile's results are stored; each
+// thread keeps its R2 stage-1 twiddles in registers for all tiles.  Every
+// wait is bounded: on timeout the
 // kernel records an error code in the status word, waits (bounded) once more
 // for its own MMAs and frees its tensor memory before returning.
 #include <cuda_fp16.h>
@@ -142,8 +143,8 @@ struct TcShape {
     static constexpr int OFF_A1H = 2 * (B1 + B2), OFF_A1L = OFF_A1H + A1;
     static constexpr int OFF_A2H = OFF_A1H, OFF_A2L = OFF_A2H + A2;
     static constexpr int A_REGION = 2 * (A1 > A2 ? A1 : A2);
-    static constexpr int OFF_SCALE = OFF_A1H + A_REGION;           // S floats
-    static constexpr int OFF_BAR = (OFF_SCALE + 4 * S + 15) & ~15;  // mbarrier + tmem slot
+    static constexpr int OFF_SCALE = OFF_A1H + A_REGION;           // 2 x S floats
+    static constexpr int OFF_BAR = (OFF_SCALE + 8 * S + 15) & ~15;  // mbarrier + tmem slot
     static constexpr int SMEM = OFF_BAR + 16;
     static constexpr int COLS_USED = N1 + G2 * N2;
     static constexpr int TMEM_COLS = COLS_USED <= 32 ? 32 : COLS_USED <= 64 ? 64 : COLS_USED <= 128 ? 128 : 256;
@@ -219,8 +220,10 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
     for (int k2 = 0; k2 < R2; ++k2) tw[k2] = __ldg(&A.tw[(n1 * k2) % SH::M]);
     float2 x[R2];
     tc_load_input<R1, R2>(A, (i64)blockIdx.x, s1, n1, x);
-    for (i64 tile = blockIdx.x; tile < A.ntiles && !failed; tile += gridDim.x) {
-        const i64 sig0 = tile * SH::S;
+    // Stage 1 of tile tl: operand from x (its scale in slot b of scale_inv),
+    // MMAs issued and committed, then the input of tile tl + gridDim.x loaded
+    // into x so its loads are in flight while tile tl multiplies and writes.
+    auto stage1 = [&](i64 tl, int b) {
         // ---- stage 1 operand: row t = (s1, n1), k = 2*n2 + {re, im} ----
         {
             float amax = 0.f;
@@ -232,7 +235,7 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
             const float sc = pow2_scale(amax, e);
             // stage-1 results are below 2 R2 2^14 in these units; stage 2 works on
             // them times 2^-6, so its results carry the factor 2^(14-e-6)
-            if (n1 == 0) scale_inv[s1] = __uint_as_float((uint32_t)(127 + e - 8) << 23);
+            if (n1 == 0) scale_inv[b * SH::S + s1] = __uint_as_float((uint32_t)(127 + e - 8) << 23);
 #pragma unroll
             for (int kg = 0; kg < SH::K1 / 8; ++kg) {
                 __half h[8], l[8];
@@ -267,9 +270,18 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
             }
             tc_commit(bar);
         }
-        // x is in the stage-1 operand: load the next tile's input now, so its
-        // loads are in flight while this tile multiplies and writes
-        tc_load_input<R1, R2>(A, tile + gridDim.x, s1, n1, x);
+        tc_load_input<R1, R2>(A, tl + gridDim.x, s1, n1, x);
+    };
+    // Tiles are software-pipelined by one stage: a tile's stage-1 MMAs are
+    // issued before the previous tile's results are read out of tensor memory
+    // and stored (its operand region and columns [0, N1) are free by then:
+    // the previous tile's stage-2 MMAs have completed), so they run during
+    // those stores.  One MMA group is in flight at a time, so one mbarrier
+    // with alternating phases tracks them.
+    if ((i64)blockIdx.x < A.ntiles) stage1((i64)blockIdx.x, 0);
+    int buf = 0;
+    for (i64 tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x, buf ^= 1) {
+        const i64 sig0 = tile * SH::S;
         // every thread leaves together when a wait times out
         if (__syncthreads_or(!mbar_wait_bounded(bar, phase))) { failed = true; break; }
         phase ^= 1;
@@ -323,6 +335,7 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
         if (__syncthreads_or(!mbar_wait_bounded(bar, phase))) { failed = true; break; }
         phase ^= 1;
         tc_fence_after();
+        if (tile + gridDim.x < A.ntiles) stage1(tile + gridDim.x, buf ^ 1);
         // ---- stage-2 results: lane row r2 = (s, k2) holds X[k1*R2 + k2], k1 = 0..R1-1 ----
 #pragma unroll
         for (int g = 0; g < SH::G2; ++g) {
@@ -330,7 +343,7 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
             const int s = r2 / R2, k2 = r2 % R2;
             const i64 sig = sig0 + s;
             const bool live = s < SH::S && sig < A.nsig;
-            const float un = live ? scale_inv[s] : 0.f;
+            const float un = live ? scale_inv[buf * SH::S + s] : 0.f;
 #pragma unroll
             for (int c0 = 0; c0 < SH::N2; c0 += 16) {
                 float acc[16];
@@ -345,9 +358,6 @@ __global__ void __launch_bounds__(128) fft_tc_kernel(TcArgs A) {
                 }
             }
         }
-        tc_fence_before();
-        __syncthreads();   // TMEM and A operands are rewritten by the next tile
-        tc_fence_after();
     }
     if (failed) {
         if (t == 0) report_status(A.status, 2);

@@ -33,7 +33,7 @@ def shape(R1, R2):
     # the stage-1 and stage-2 A operands (hi + lo each) share one region
     a_region = 2 * max(A1, A2)
     off_scale = 2 * (B1 + B2) + a_region
-    smem = ((off_scale + 4 * S + 15) & ~15) + 16
+    smem = ((off_scale + 8 * S + 15) & ~15) + 16   # two slots of S row scales
     cols = N1 + G2 * N2
     tmem = next(c for c in (32, 64, 128, 256) if cols <= c)
     return dict(S=S, K1=K1, K2=K2, N1=N1, N2=N2, G2=G2, SB=SB, A1=A1, A2=A2, a_region=a_region,
