@@ -22,9 +22,9 @@
 // shared memory, so they are in flight while this tile multiplies and writes;
 // the next tile's stage-1 MMAs run while this tile's results are stored; each
 // thread keeps its R2 stage-1 twiddles in registers for all tiles.  Every
-// wait is bounded: on timeout the
-// kernel records an error code in the status word, waits (bounded) once more
-// for its own MMAs and frees its tensor memory before returning.
+// wait is bounded: on timeout the kernel records an error code in the status
+// word, waits (bounded) once more for its own MMAs and frees its tensor
+// memory before returning.
 #include <cuda_fp16.h>
 
 #include <algorithm>
