@@ -3,8 +3,8 @@ fft_tc_kernel / TcShape): the two DFT-matrix GEMM stages with the kernel's
 operand indices give the DFT of each row, the stage-2 A operand's padded
 core-matrix strides place every (row, K) element once inside its buffer, the
 32 lanes of a warp write that operand without shared-memory bank conflicts,
-and the kernel's shared memory and tensor memory admit three or four CTAs
-per SM."""
+the kernel's shared memory and tensor memory admit three or four CTAs per
+SM, and the rotated tile loop's mbarrier phases and row-scale slots line up."""
 import numpy as np
 import pytest
 
@@ -127,3 +127,64 @@ def test_two_stage_gemm_matches_dft(R1, R2, sign):
         out[s, np.arange(R1) * R2 + k2] = D2[r2, 0::2] + 1j * D2[r2, 1::2]
     ref = np.fft.fft(x, axis=1) if sign < 0 else np.fft.ifft(x, axis=1) * m
     assert np.abs(out - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+def _rotated_schedule(cta, grid, ntiles):
+    """Event list of one CTA of the tensor-core kernel's rotated tile loop:
+    ("commit", group, tile), ("wait", parity), ("scale_w", slot, tile),
+    ("scale_r", slot, tile)."""
+    ev = []
+    phase = 0
+
+    def stage1(tl, b):
+        ev.append(("scale_w", b, tl))
+        ev.append(("commit", "mma1", tl))
+
+    if cta < ntiles:
+        stage1(cta, 0)
+    buf = 0
+    tile = cta
+    while tile < ntiles:
+        ev.append(("wait", phase, "mma1", tile))
+        phase ^= 1
+        ev.append(("commit", "mma2", tile))
+        ev.append(("wait", phase, "mma2", tile))
+        phase ^= 1
+        if tile + grid < ntiles:
+            stage1(tile + grid, buf ^ 1)
+        ev.append(("scale_r", buf, tile))
+        tile += grid
+        buf ^= 1
+    return ev
+
+
+@pytest.mark.parametrize("grid,ntiles", [(1, 1), (1, 5), (3, 3), (3, 10), (4, 17), (456, 1365)])
+def test_rotated_loop_bookkeeping(grid, ntiles):
+    """The rotated loop keeps one MMA group in flight at a time, so one
+    mbarrier with alternating parity serves both stages: every wait is for
+    the group committed just before it, with the parity of that completion;
+    a tile's results are scaled by the slot its own stage 1 wrote, and no slot
+    is rewritten before it is read; nothing is in flight at a normal exit."""
+    for cta in range(min(grid, ntiles)):
+        ev = _rotated_schedule(cta, grid, ntiles)
+        outstanding = None
+        completions = 0
+        slots = {}
+        for e in ev:
+            if e[0] == "commit":
+                assert outstanding is None, "two MMA groups in flight"
+                outstanding = (e[1], e[2])
+            elif e[0] == "wait":
+                assert outstanding == (e[2], e[3])
+                assert e[1] == completions % 2          # parity of this completion
+                completions += 1
+                outstanding = None
+            elif e[0] == "scale_w":
+                assert slots.get(e[1]) is None, "slot rewritten before it was read"
+                slots[e[1]] = e[2]
+            elif e[0] == "scale_r":
+                assert slots.get(e[1]) == e[2]
+                slots[e[1]] = None
+        assert outstanding is None
+        tiles = list(range(cta, ntiles, grid))
+        assert [e[2] for e in ev if e[0] == "scale_r"] == tiles
