@@ -469,7 +469,7 @@ dtfft_error_t tc_create(int m, void** out) {
         // query answers 1 for this kernel, so the count is made here.
         // Measured on 1 GiB batches of 256/512/768/1024-point rows: one CTA
         // per SM 617/525/590/568 us, two 461/495/525/502 us, 5/3/3/3
-        // 409/438/457/437 us.  DTFFT_GB_TC_CTAS=k sets a lower limit
+        // 409/438/457/437 us.  DTFFT_GB_TC_CTAS=k caps the count at k
         // (experiments).
         int cap = 8;
         if (const char* ce = getenv("DTFFT_GB_TC_CTAS"))
